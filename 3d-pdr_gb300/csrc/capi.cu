@@ -1,0 +1,367 @@
+// capi.cu -- the C ABI of lib3dpdr_gb300.so (declared in include/pdrgpu.h).
+//
+// calculate_abundances_ keeps the reference's symbol, arguments and status
+// semantics (calculate_abundances.c:64-354); the batched entry points take
+// device arrays and a stream so a caller can keep state resident in HBM and
+// capture the calls in a CUDA graph.
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "pdr_internal.h"
+
+extern "C" {
+// Fortran module variables the reference binds to C (modules.F90:165-166,383,
+// 529-530).  Declared weak so the library also loads in programs that are not
+// the 3D-PDR driver; calculate_abundances_ then reports that they are missing.
+extern double chemistry_module_mp_relative_abundance_tolerance_ __attribute__((weak));
+extern double chemistry_module_mp_absolute_abundance_tolerance_ __attribute__((weak));
+extern double maincode_module_mp_start_time_ __attribute__((weak));
+extern double maincode_module_mp_end_time_ __attribute__((weak));
+extern int global_module_mp_nelect_ __attribute__((weak));
+}
+
+namespace pdr {
+
+size_t chem_warp_smem_per_warp(int nsp, int nreac, int nparts, bool mixed);
+int launch_chem_warp(const pdr_net *net, int ncell, double *ab, const double *rate, const double *dens,
+                     const double *tend, const pdr_chem_opts &o, int *status, int *stats, int *queue,
+                     int *fb_list, int *fb_count, const int *cell_list, const int *total_ptr, bool mixed,
+                     int sm_count, cudaStream_t st);
+int launch_rates(const pdr_net *net, const pdr_phys &ph, int ncell, int nrays, const double *T,
+                 const double *Td, const double *rad, const double *AV, const double *col5, double *rate,
+                 int *status, int sm_count, cudaStream_t st);
+int launch_chem_eval(const pdr_net *net, int nstate, const double *x, const double *rate, const double *dens,
+                     double *out, double *xe_out, int mode, cudaStream_t st);
+int upload_shield_tables(int dev);
+void shield_tables_host(double *xderiv30, double *scoderiv48);
+
+static thread_local std::string g_err;
+
+void set_error(const std::string &msg) { g_err = msg; }
+
+int cuda_fail(cudaError_t e, const char *what) {
+  set_error(std::string(what) + ": " + cudaGetErrorString(e));
+  return PDR_E_CUDA;
+}
+
+static int current_device(int *dev, int *sms) {
+  int d = 0;
+  cudaError_t e = cudaGetDevice(&d);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  int n = 0;
+  e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, d);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceGetAttribute");
+  *dev = d;
+  *sms = n;
+  return 0;
+}
+
+// Per-device scratch of the batched solver: the work-queue cursors, the
+// FP64-redo list of the mixed form and its count.  Grown on demand, never
+// shrunk; a call made during stream capture must not need to grow it.
+struct Scratch {
+  int *counters = nullptr;   // [0] queue, [1] redo queue, [2] redo count
+  int *redo = nullptr;
+  size_t redo_cap = 0;
+};
+static std::mutex g_mu;
+static Scratch g_scratch[64];
+
+static int scratch_for(int dev, size_t ncell, Scratch **out) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Scratch &s = g_scratch[dev & 63];
+  if (!s.counters) {
+    cudaError_t e = cudaMalloc(&s.counters, 4 * sizeof(int));
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(scratch)");
+  }
+  if (s.redo_cap < ncell) {
+    if (s.redo) cudaFree(s.redo);
+    s.redo = nullptr;
+    size_t cap = ncell < 1024 ? 1024 : ncell;
+    cudaError_t e = cudaMalloc(&s.redo, cap * sizeof(int));
+    if (e != cudaSuccess) { s.redo_cap = 0; return cuda_fail(e, "cudaMalloc(redo list)"); }
+    s.redo_cap = cap;
+  }
+  *out = &s;
+  return 0;
+}
+
+}  // namespace pdr
+
+using namespace pdr;
+
+extern "C" {
+
+const char *pdr_last_error(void) { return g_err.c_str(); }
+
+void pdr_chem_opts_default(pdr_chem_opts *o) {
+  if (!o) return;
+  o->reltol = 1.0e-8;
+  o->abstol = 1.0e-30;
+  o->start_time_yr = 0.0;
+  o->end_time_yr = 1.0e7;
+  o->mxstep = 10000000L;
+  o->precision = PDR_FP64;
+  o->warps_per_block = 0;
+  o->blocks_per_sm = 0;
+}
+
+int pdr_device_info(int *sm_count, int *cc_major, int *cc_minor) {
+  int dev = 0, sms = 0;
+  int rc = current_device(&dev, &sms);
+  if (rc) return rc;
+  if (sm_count) *sm_count = sms;
+  int a = 0, b = 0;
+  cudaDeviceGetAttribute(&a, cudaDevAttrComputeCapabilityMajor, dev);
+  cudaDeviceGetAttribute(&b, cudaDevAttrComputeCapabilityMinor, dev);
+  if (cc_major) *cc_major = a;
+  if (cc_minor) *cc_minor = b;
+  return 0;
+}
+
+int pdr_net_load(const char *species_path, const char *rates_path, const char *layout_path, pdr_net **out) {
+  if (!species_path || !rates_path || !out) { set_error("pdr_net_load: null argument"); return PDR_E_ARG; }
+  pdr_net *net = new pdr_net();
+  std::string err = load_network(species_path, rates_path, layout_path, net->host);
+  if (!err.empty()) { set_error(err); delete net; return PDR_E_IO; }
+  int dev = 0, sms = 0;
+  int rc = current_device(&dev, &sms);
+  if (rc == 0) rc = upload_shield_tables(dev);
+  if (rc == 0) rc = build_device_tables(net);
+  if (rc) { pdr_net_free(net); return rc; }
+  net->device = dev;
+  *out = net;
+  return 0;
+}
+
+void pdr_net_free(pdr_net *net) {
+  if (!net) return;
+  for (void *p : net->allocations) cudaFree(p);
+  delete net;
+}
+
+int pdr_net_info(const pdr_net *net, int *nspec, int *nreac, int *neq) {
+  if (!net) { set_error("pdr_net_info: null network"); return PDR_E_ARG; }
+  if (nspec) *nspec = net->host.nspec;
+  if (nreac) *nreac = net->host.nreac;
+  if (neq) *neq = net->host.neq;
+  return 0;
+}
+
+int pdr_net_special_reactions(const pdr_net *net, int nr[6]) {
+  if (!net || !nr) { set_error("pdr_net_special_reactions: null argument"); return PDR_E_ARG; }
+  for (int k = 0; k < 6; k++) nr[k] = net->host.nr[k];
+  return 0;
+}
+
+static std::vector<pdr_net *> g_registered;
+
+int pdr_net_register(pdr_net *net) {
+  if (!net) { set_error("pdr_net_register: null network"); return PDR_E_ARG; }
+  std::lock_guard<std::mutex> lk(g_mu);
+  g_registered.push_back(net);
+  return 0;
+}
+
+int pdr_chem_solve_batched(const pdr_net *net, int ncell, double *d_abundance, const double *d_rate,
+                           const double *d_density, const double *d_t_end_yr, const pdr_chem_opts *opts,
+                           int *d_status, int *d_stats, void *stream) {
+  if (!net || ncell < 0 || !d_abundance || !d_rate || !d_density || !d_status) {
+    set_error("pdr_chem_solve_batched: invalid argument");
+    return PDR_E_ARG;
+  }
+  if (ncell == 0) return 0;
+  pdr_chem_opts o;
+  pdr_chem_opts_default(&o);
+  if (opts) o = *opts;
+  if (!(o.reltol >= 0.0) || !(o.abstol > 0.0) || o.mxstep <= 0 ||
+      (o.precision != PDR_FP64 && o.precision != PDR_MIXED)) {
+    set_error("pdr_chem_solve_batched: invalid options");
+    return PDR_E_ARG;
+  }
+  if (!net->warp_ok || net->host.neq != 32) {
+    set_error("pdr_chem_solve_batched: this build integrates networks with 32 ODE species");
+    return PDR_E_NET;
+  }
+  int dev = 0, sms = 0;
+  int rc = current_device(&dev, &sms);
+  if (rc) return rc;
+  Scratch *s = nullptr;
+  rc = scratch_for(dev, (size_t)ncell, &s);
+  if (rc) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e = cudaMemsetAsync(s->counters, 0, 4 * sizeof(int), st);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(scratch)");
+  const bool mixed = (o.precision == PDR_MIXED);
+  rc = launch_chem_warp(net, ncell, d_abundance, d_rate, d_density, d_t_end_yr, o, d_status, d_stats,
+                        s->counters + 0, s->redo, s->counters + 2, nullptr, nullptr, mixed, sms, st);
+  if (rc) return rc;
+  if (mixed) {
+    // cells whose FP32 Newton iteration failed are re-solved in FP64
+    rc = launch_chem_warp(net, ncell, d_abundance, d_rate, d_density, d_t_end_yr, o, d_status, d_stats,
+                          s->counters + 1, nullptr, nullptr, s->redo, s->counters + 2, false, sms, st);
+    if (rc) return rc;
+  }
+  return 0;
+}
+
+int pdr_rates_batched(const pdr_net *net, const pdr_phys *phys, int ncell, int nrays, const double *d_T,
+                      const double *d_Td, const double *d_rad_surface, const double *d_AV,
+                      const double *d_column5, double *d_rate, int *d_status, void *stream) {
+  if (!net || !phys || ncell < 0 || nrays <= 0 || !d_T || !d_Td || !d_rad_surface || !d_AV ||
+      !d_column5 || !d_rate) {
+    set_error("pdr_rates_batched: invalid argument");
+    return PDR_E_ARG;
+  }
+  if (ncell == 0) return 0;
+  int dev = 0, sms = 0;
+  int rc = current_device(&dev, &sms);
+  if (rc) return rc;
+  rc = upload_shield_tables(dev);
+  if (rc) return rc;
+  return launch_rates(net, *phys, ncell, nrays, d_T, d_Td, d_rad_surface, d_AV, d_column5, d_rate,
+                      d_status, sms, (cudaStream_t)stream);
+}
+
+// Diagnostic: the device RHS f(x) (mode 0, d_out[nstate*neq], d_xe[nstate]) or the
+// analytic Jacobian (mode 1, d_out[nstate*neq*neq] row-major) at given states.
+int pdr_chem_eval_batched(const pdr_net *net, int nstate, const double *d_x, const double *d_rate,
+                          const double *d_density, int mode, double *d_out, double *d_xe, void *stream) {
+  if (!net || nstate < 0 || !d_x || !d_rate || !d_density || !d_out || (mode != 0 && mode != 1)) {
+    set_error("pdr_chem_eval_batched: invalid argument");
+    return PDR_E_ARG;
+  }
+  if (!net->warp_ok || net->host.neq != 32) {
+    set_error("pdr_chem_eval_batched: this build evaluates networks with 32 ODE species");
+    return PDR_E_NET;
+  }
+  if (nstate == 0) return 0;
+  return launch_chem_eval(net, nstate, d_x, d_rate, d_density, d_out, d_xe, mode, (cudaStream_t)stream);
+}
+
+// diagnostic export of the shielding spline tables (tests compare them with the oracle)
+int pdr_shield_tables(double *xderiv30, double *scoderiv48) {
+  if (!xderiv30 || !scoderiv48) { set_error("pdr_shield_tables: null argument"); return PDR_E_ARG; }
+  shield_tables_host(xderiv30, scoderiv48);
+  return 0;
+}
+
+// ---------------- legacy calculate_abundances_ ----------------
+
+static pdr_net *find_network(int nspec, int nreac) {
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    for (pdr_net *n : g_registered)
+      if (n->host.nspec == nspec && n->host.nreac == nreac) return n;
+  }
+  const char *dir = std::getenv("PDR_NETWORK_DIR");
+  std::string base = dir ? std::string(dir) : std::string(".");
+  const char *names[3] = {"reduced", "full", "mynetwork"};
+  for (const char *nm : names) {
+    std::string sp = base + "/species_" + nm + ".d", rp = base + "/rates_" + nm + ".d";
+    std::string lp = base + "/layout_" + nm + ".d";
+    FILE *f = std::fopen(sp.c_str(), "r");
+    if (!f) continue;
+    std::fclose(f);
+    FILE *fl = std::fopen(lp.c_str(), "r");
+    if (fl) std::fclose(fl);
+    pdr_net *n = nullptr;
+    if (pdr_net_load(sp.c_str(), rp.c_str(), fl ? lp.c_str() : nullptr, &n) != 0) continue;
+    if (n->host.nspec == nspec && n->host.nreac == nreac) {
+      pdr_net_register(n);
+      return n;
+    }
+    pdr_net_free(n);
+  }
+  return nullptr;
+}
+
+struct LegacyBuffers {
+  double *ab = nullptr, *rate = nullptr, *dens = nullptr;
+  int *status = nullptr;
+  size_t ab_n = 0, rate_n = 0, dens_n = 0, status_n = 0;
+};
+static LegacyBuffers g_legacy[64];
+
+static int grow(void **p, size_t &have, size_t need, size_t elem) {
+  if (have >= need) return 0;
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  cudaError_t e = cudaMalloc(p, need * elem);
+  if (e != cudaSuccess) { have = 0; return cuda_fail(e, "cudaMalloc(calculate_abundances_ buffers)"); }
+  have = need;
+  return 0;
+}
+
+int pdr_calculate_abundances(pdr_net *net, double *abundance, double *rate, double *density,
+                             double *temperature, int npart, int nspec, int nreac, const pdr_chem_opts *opts) {
+  (void)temperature;
+  if (!abundance || !rate || !density || npart < 0) {
+    set_error("pdr_calculate_abundances: invalid argument");
+    return PDR_E_ARG;
+  }
+  if (npart == 0) return 0;
+  if (!net) net = find_network(nspec, nreac);
+  if (!net || net->host.nspec != nspec || net->host.nreac != nreac) {
+    set_error("pdr_calculate_abundances: no network with the call's nspec/nreac is registered or found");
+    return PDR_E_NET;
+  }
+  const int n = npart, ns = nspec, nr = nreac;
+  int dev = 0, sms = 0;
+  int rc = current_device(&dev, &sms);
+  if (rc) return rc;
+  LegacyBuffers &b = g_legacy[dev & 63];
+  if ((rc = grow((void **)&b.ab, b.ab_n, (size_t)n * ns, sizeof(double)))) return rc;
+  if ((rc = grow((void **)&b.rate, b.rate_n, (size_t)n * nr, sizeof(double)))) return rc;
+  if ((rc = grow((void **)&b.dens, b.dens_n, (size_t)n, sizeof(double)))) return rc;
+  if ((rc = grow((void **)&b.status, b.status_n, (size_t)n, sizeof(int)))) return rc;
+  cudaStream_t st = nullptr;
+  cudaError_t e;
+  if ((e = cudaMemcpyAsync(b.ab, abundance, (size_t)n * ns * sizeof(double), cudaMemcpyHostToDevice, st)) ||
+      (e = cudaMemcpyAsync(b.rate, rate, (size_t)n * nr * sizeof(double), cudaMemcpyHostToDevice, st)) ||
+      (e = cudaMemcpyAsync(b.dens, density, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, st)))
+    return cuda_fail(e, "calculate_abundances: host-to-device copy");
+  rc = pdr_chem_solve_batched(net, n, b.ab, b.rate, b.dens, nullptr, opts, b.status, nullptr, st);
+  if (rc) return rc;
+  std::vector<int> status(n);
+  if ((e = cudaMemcpyAsync(abundance, b.ab, (size_t)n * ns * sizeof(double), cudaMemcpyDeviceToHost, st)) ||
+      (e = cudaMemcpyAsync(status.data(), b.status, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost, st)) ||
+      (e = cudaStreamSynchronize(st)))
+    return cuda_fail(e, "calculate_abundances: device-to-host copy");
+  int result = 0;
+  for (int i = 0; i < n; i++)
+    if (status[i] != 0) result = status[i];
+  return result;
+}
+
+int calculate_abundances_(double *abundance, double *rate, double *density, double *temperature, int *npart,
+                          int *nspec, int *nreac) {
+  if (!abundance || !rate || !density || !npart || !nspec || !nreac || *npart < 0) {
+    set_error("calculate_abundances_: invalid argument");
+    return PDR_E_ARG;
+  }
+  if (!&chemistry_module_mp_relative_abundance_tolerance_ || !&chemistry_module_mp_absolute_abundance_tolerance_ ||
+      !&maincode_module_mp_start_time_ || !&maincode_module_mp_end_time_ || !&global_module_mp_nelect_) {
+    set_error("calculate_abundances_: the Fortran module variables (chemistry_module_mp_*, "
+              "maincode_module_mp_*, global_module_mp_nelect_) are not defined by the caller");
+    return PDR_E_ARG;
+  }
+  if (global_module_mp_nelect_ != *nspec) {
+    set_error("calculate_abundances_: the electron must be the last species");
+    return PDR_E_NET;
+  }
+  pdr_chem_opts o;
+  pdr_chem_opts_default(&o);
+  o.reltol = chemistry_module_mp_relative_abundance_tolerance_;
+  o.abstol = chemistry_module_mp_absolute_abundance_tolerance_;
+  o.start_time_yr = maincode_module_mp_start_time_;
+  o.end_time_yr = maincode_module_mp_end_time_;
+  if (const char *p = std::getenv("PDR_PRECISION")) o.precision = (std::strcmp(p, "mixed") == 0) ? PDR_MIXED : PDR_FP64;
+  return pdr_calculate_abundances(nullptr, abundance, rate, density, temperature, *npart, *nspec, *nreac, &o);
+}
+
+}  // extern "C"

@@ -1,0 +1,88 @@
+// pdr_internal.h -- host-side network model and device table layouts shared by
+// the CUDA translation units of lib3dpdr_gb300.so.
+#pragma once
+
+#include <array>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/pdrgpu.h"
+
+namespace pdr {
+
+// ODE kinds of a reaction (how it enters the generated RHS, odes_<net>.c)
+enum OdeKind { ODE_UNI = 0, ODE_BI = 1, ODE_GRAINH2 = 2, ODE_XRAY = 3 };
+
+// rate-evaluator branches of calc_reac_rates.F90:53-378
+enum RateKind {
+  RK_THERMAL = 0, RK_H2FORM, RK_PAH, RK_PHOTO_H2, RK_PHOTO_HD, RK_PHOTO_CO, RK_PHOTO_CI,
+  RK_PHOTO_SI, RK_PHOTO, RK_CRP, RK_CRPHOT, RK_FREEZE, RK_ELFRZE, RK_CRH, RK_PHOTD, RK_THERM,
+  RK_GRAIN, RK_XRAY
+};
+
+constexpr int kWarp = 32;
+
+// Device tables of one network for the warp-per-cell integrator (neq <= 32).
+// Slot convention: 0..neq-1 species, neq = electron (x_e), neq+1 = constant 1.
+struct WarpTables {
+  int neq = 0, nreac = 0;
+  int rhs_len = 0;     // RHS terms per lane (balanced chunks)
+  int nparts = 0;      // partial-sum slots (slot nparts is a constant zero)
+  int plist_len = 0;   // partial slots summed per species
+  int jac_len = 0;     // Jacobian terms per species (padded)
+  int2 *rab = nullptr;        // [nreac] reactant slots (a, b)
+  double *nh_mask = nullptr;  // [nreac] 1 if the rate constant is multiplied by n_H
+  int *rhs_r = nullptr;       // [rhs_len][32] reaction of each term
+  double *rhs_nu = nullptr;   // [rhs_len][32] stoichiometric coefficient (0 = padding)
+  int *rhs_flush = nullptr;   // [rhs_len][32] partial slot written after the term, -1 none
+  int *plist = nullptr;       // [plist_len][32] partial slots of species `lane`
+  int *jac_r = nullptr;       // [jac_len][32]
+  double *jac_nu = nullptr;   // [jac_len][32]
+  float *jac_nu_f = nullptr;  // [jac_len][32]
+  double *xe_coef = nullptr;  // [32] electron-sum coefficient per slot
+};
+
+// Device tables for the rate evaluator.
+struct RateTables {
+  int nreac = 0;
+  int *kind = nullptr;        // RateKind
+  int *dup = nullptr;         // DUPLICATE
+  int *dup_next = nullptr;    // DUPLICATE(I+1) or -1 past the end
+  double *alpha = nullptr, *beta = nullptr, *gamma = nullptr, *rtmin = nullptr, *rtmax = nullptr;
+  int *flags = nullptr;       // bit0: reactant-1 name starts with 'G'; bit1: H2 photo sets NRH2;
+                              // bit2: HD photo sets NRHD
+};
+
+struct HostNet {
+  int nspec = 0, nreac = 0, neq = 0;
+  std::vector<std::string> spec;     // species-file names
+  std::vector<std::string> slot;     // species each ODE slot represents in the RHS
+  std::vector<int> xe;               // electron-sum coefficient per slot
+  std::vector<std::array<std::string, 3>> reac;
+  std::vector<std::array<std::string, 4>> prod;
+  std::vector<double> alpha, beta, gamma, rtmin, rtmax;
+  std::vector<int> dup, ode_kind, rate_kind, ra, rb;
+  std::vector<std::array<int, 4>> pidx;
+  int nr[6] = {0, 0, 0, 0, 0, 0};    // NRGR, NRH2, NRHD, NRCO, NRCI, NRSI (1-based)
+};
+
+std::string load_network(const char *species, const char *rates, const char *layout, HostNet &net);
+
+}  // namespace pdr
+
+struct pdr_net {
+  pdr::HostNet host;
+  int device = -1;
+  bool warp_ok = false;
+  pdr::WarpTables warp;
+  pdr::RateTables rates;
+  std::vector<void *> allocations;
+};
+
+namespace pdr {
+void set_error(const std::string &msg);
+int cuda_fail(cudaError_t e, const char *what);
+int build_device_tables(pdr_net *net);
+}  // namespace pdr

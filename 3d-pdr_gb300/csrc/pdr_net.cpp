@@ -1,0 +1,297 @@
+// pdr_net.cpp -- network loader and device-table builder.
+//
+// Parses the reference's network files with the semantics of
+// read_species.F90:15-194 and read_rates.F90:9-95 (CSV records, empty fields
+// keep their blank/zero initial values, consecutive identical reactions form a
+// duplicate group whose RTMIN is moved to the previous RTMAX, :61-74), classifies
+// every reaction the way calc_reac_rates.F90:53-112 dispatches it, and builds the
+// tables the kernels read: reactant slots per reaction, the net stoichiometry as
+// per-species term lists, and their balanced split over the 32 lanes of a warp.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <sstream>
+
+#include "pdr_internal.h"
+
+namespace pdr {
+
+static std::string trim(const std::string &s) {
+  size_t b = s.find_first_not_of(" \t\r\n"), e = s.find_last_not_of(" \t\r\n");
+  return b == std::string::npos ? std::string() : s.substr(b, e - b + 1);
+}
+
+static std::vector<std::string> csv(const std::string &line) {
+  std::vector<std::string> f;
+  std::string cur;
+  for (char c : line) {
+    if (c == ',') { f.push_back(trim(cur)); cur.clear(); }
+    else cur.push_back(c);
+  }
+  f.push_back(trim(cur));
+  return f;
+}
+
+static std::vector<std::string> records(const char *path, std::string &err) {
+  std::vector<std::string> out;
+  std::ifstream in(path);
+  if (!in) { err = std::string("cannot open ") + path; return out; }
+  std::string line;
+  while (std::getline(in, line))
+    if (!trim(line).empty()) out.push_back(line);
+  return out;
+}
+
+static double num(const std::string &s) { return s.empty() ? 0.0 : std::strtod(s.c_str(), nullptr); }
+
+static int name_charge(const std::string &s) {
+  if (s == "e-" || s == "ELECTR") return -1;
+  int q = 0;
+  for (char c : s) q += (c == '+') - (c == '-');
+  return q;
+}
+
+std::string load_network(const char *species, const char *rates, const char *layout, HostNet &net) {
+  std::string err;
+  auto sp = records(species, err);
+  if (!err.empty()) return err;
+  for (auto &r : sp) {
+    auto f = csv(r);
+    if (f.size() < 4) return "bad species record";
+    net.spec.push_back(f[1]);
+  }
+  net.nspec = (int)net.spec.size();
+  net.neq = net.nspec - 1;
+  if (net.nspec < 2 || (net.spec.back() != "e-" && net.spec.back() != "ELECTR"))
+    return "the electron must be the last species (calculate_abundances.c:67)";
+  net.slot.assign(net.spec.begin(), net.spec.end() - 1);
+  net.xe.resize(net.neq);
+  for (int i = 0; i < net.neq; i++) net.xe[i] = name_charge(net.spec[i]);
+  if (layout) {
+    auto ly = records(layout, err);
+    if (!err.empty()) return err;
+    if ((int)ly.size() != net.neq) return "layout slot count does not match the species file";
+    for (auto &r : ly) {
+      auto f = csv(r);
+      if (f.size() < 4) return "bad layout record";
+      int s = std::atoi(f[0].c_str()) - 1;
+      if (s < 0 || s >= net.neq || f[1] != net.spec[s]) return "layout does not match the species file";
+      net.slot[s] = f[2];
+      net.xe[s] = std::atoi(f[3].c_str());
+    }
+  }
+  std::map<std::string, int> slot_of;
+  for (int i = 0; i < net.neq; i++) slot_of[net.slot[i]] = i;
+  slot_of[net.spec.back()] = net.neq;  // electron
+
+  auto rr = records(rates, err);
+  if (!err.empty()) return err;
+  net.nreac = (int)rr.size();
+  const int n = net.nreac;
+  net.reac.resize(n); net.prod.resize(n);
+  net.alpha.resize(n); net.beta.resize(n); net.gamma.resize(n);
+  net.rtmin.resize(n); net.rtmax.resize(n); net.dup.assign(n, 0);
+  net.ode_kind.resize(n); net.rate_kind.resize(n); net.ra.resize(n); net.rb.resize(n);
+  net.pidx.resize(n);
+  for (int i = 0; i < n; i++) {
+    auto f = csv(rr[i]);
+    if (f.size() < 14) return "bad rate record " + std::to_string(i + 1);
+    for (int k = 0; k < 3; k++) net.reac[i][k] = f[1 + k];
+    for (int k = 0; k < 4; k++) net.prod[i][k] = f[4 + k];
+    net.alpha[i] = num(f[8]); net.beta[i] = num(f[9]); net.gamma[i] = num(f[10]);
+    net.rtmin[i] = num(f[12]); net.rtmax[i] = num(f[13]);
+    if (i > 0 && net.reac[i] == net.reac[i - 1] && net.prod[i] == net.prod[i - 1]) {
+      if (net.dup[i - 1] == 0) net.dup[i - 1] = 1;
+      net.dup[i] = net.dup[i - 1] + 1;
+      net.rtmin[i] = net.rtmax[i - 1];
+    }
+  }
+  auto is = [](const std::string &a, const char *b) { return a == b; };
+  for (int i = 0; i < n; i++) {
+    const auto &R = net.reac[i];
+    const auto &P = net.prod[i];
+    const std::string &r2 = R[1];
+    bool xray = is(r2, "XRAY") || is(r2, "XRSEC") || is(r2, "XRLYA") || is(r2, "XRPHOT");
+    bool uni = is(r2, "PHOTON") || is(r2, "CRP") || is(r2, "CRPHOT") || r2.empty() ||
+               is(r2, "FREEZE") || is(r2, "ELFRZE") || is(r2, "CRH") || is(r2, "PHOTD") ||
+               is(r2, "THERM") || (!r2.empty() && r2[0] == '#');
+    auto sl = [&](const std::string &s) { auto it = slot_of.find(s); return it == slot_of.end() ? -1 : it->second; };
+    net.ra[i] = sl(R[0]);
+    net.rb[i] = -1;
+    if (xray) net.ode_kind[i] = ODE_XRAY;
+    else if (R[2] == "#") net.ode_kind[i] = ODE_GRAINH2;
+    else if (uni) net.ode_kind[i] = ODE_UNI;
+    else { net.ode_kind[i] = ODE_BI; net.rb[i] = sl(R[1]); }
+    if (net.ra[i] < 0 || (net.ode_kind[i] == ODE_BI && net.rb[i] < 0))
+      return "reaction " + std::to_string(i + 1) + ": reactant is not a species";
+    for (int k = 0; k < 4; k++) net.pidx[i][k] = sl(P[k]);
+    auto anyP = [&](const char *s) { for (auto &p : P) if (p == s) return true; return false; };
+    int k;
+    if (is(r2, "PHOTON")) {
+      if (is(R[0], "H2") && R[2].empty()) k = RK_PHOTO_H2;
+      else if (is(R[0], "HD") && R[2].empty()) k = RK_PHOTO_HD;
+      else if (is(R[0], "CO") && R[2].empty() && anyP("C") && anyP("O")) k = RK_PHOTO_CO;
+      else if (is(R[0], "C") && R[2].empty() &&
+               ((is(P[0], "C+") && is(P[1], "e-")) || (is(P[0], "e-") && is(P[1], "C+"))))
+        k = RK_PHOTO_CI;
+      else if (is(R[0], "S") && R[2].empty() &&
+               ((is(P[0], "S+") && is(P[1], "e-")) || (is(P[0], "e-") && is(P[1], "S+"))))
+        k = RK_PHOTO_SI;
+      else k = RK_PHOTO;
+    } else if (is(r2, "CRP")) k = RK_CRP;
+    else if (is(r2, "CRPHOT")) k = RK_CRPHOT;
+    else if (is(r2, "FREEZE")) k = RK_FREEZE;
+    else if (is(r2, "ELFRZE")) k = RK_ELFRZE;
+    else if (is(r2, "CRH")) k = RK_CRH;
+    else if (is(r2, "PHOTD")) k = RK_PHOTD;
+    else if (is(r2, "THERM")) k = RK_THERM;
+    else if (!r2.empty() && r2[0] == '#') k = RK_GRAIN;
+    else if (xray) k = RK_XRAY;
+    else {
+      bool h2f = is(R[0], "H") && is(R[1], "H") && (R[2].empty() || is(R[2], "#")) && is(P[0], "H2") &&
+                 (P[1].empty() || is(P[1], "#"));
+      bool pah = false;
+      for (auto &x : R) pah |= is(x, "PAH") || is(x, "PAH0") || is(x, "PAH+") || is(x, "PAH-");
+      k = h2f ? RK_H2FORM : (pah ? RK_PAH : RK_THERMAL);
+    }
+    net.rate_kind[i] = k;
+    if (k == RK_H2FORM) net.nr[0] = i + 1;
+    if (k == RK_PHOTO_H2 && is(P[0], "H") && is(P[1], "H")) net.nr[1] = i + 1;
+    if (k == RK_PHOTO_HD && anyP("H") && anyP("D")) net.nr[2] = i + 1;
+    if (k == RK_PHOTO_CO) net.nr[3] = i + 1;
+    if (k == RK_PHOTO_CI) net.nr[4] = i + 1;
+    if (k == RK_PHOTO_SI) net.nr[5] = i + 1;
+  }
+  return std::string();
+}
+
+// net stoichiometry nu_{i,r} of every ODE slot, sorted by slot then reaction
+struct Term { int i, r; double nu; };
+
+static std::vector<Term> stoichiometry(const HostNet &net) {
+  std::vector<Term> t;
+  for (int r = 0; r < net.nreac; r++) {
+    if (net.ode_kind[r] == ODE_XRAY) continue;
+    std::map<int, double> nu;
+    for (int k = 0; k < 4; k++)
+      if (net.pidx[r][k] >= 0 && net.pidx[r][k] < net.neq) nu[net.pidx[r][k]] += 1.0;
+    nu[net.ra[r]] -= 1.0;
+    if (net.ode_kind[r] == ODE_BI) nu[net.rb[r]] -= 1.0;
+    if (net.ode_kind[r] == ODE_GRAINH2) nu[net.ra[r]] -= 1.0;
+    for (auto &kv : nu)
+      if (kv.first < net.neq && kv.second != 0.0) t.push_back({kv.first, r, kv.second});
+  }
+  std::stable_sort(t.begin(), t.end(), [](const Term &a, const Term &b) {
+    return a.i != b.i ? a.i < b.i : a.r < b.r;
+  });
+  return t;
+}
+
+template <class T>
+static T *upload(pdr_net *net, const std::vector<T> &v, int &rc) {
+  if (v.empty()) return nullptr;
+  T *d = nullptr;
+  cudaError_t e = cudaMalloc(&d, v.size() * sizeof(T));
+  if (e != cudaSuccess) { rc = cuda_fail(e, "cudaMalloc(network tables)"); return nullptr; }
+  net->allocations.push_back(d);
+  e = cudaMemcpy(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) rc = cuda_fail(e, "cudaMemcpy(network tables)");
+  return d;
+}
+
+int build_device_tables(pdr_net *net) {
+  const HostNet &h = net->host;
+  int rc = 0;
+  // ---- rate evaluator tables ----
+  {
+    std::vector<int> kind(h.rate_kind), dup(h.dup), dn(h.nreac), flags(h.nreac, 0);
+    for (int i = 0; i < h.nreac; i++) {
+      dn[i] = (i + 1 < h.nreac) ? h.dup[i + 1] : -1;
+      if (!h.reac[i][0].empty() && h.reac[i][0][0] == 'G') flags[i] |= 1;
+    }
+    net->rates.nreac = h.nreac;
+    net->rates.kind = upload(net, kind, rc);
+    net->rates.dup = upload(net, dup, rc);
+    net->rates.dup_next = upload(net, dn, rc);
+    net->rates.alpha = upload(net, h.alpha, rc);
+    net->rates.beta = upload(net, h.beta, rc);
+    net->rates.gamma = upload(net, h.gamma, rc);
+    net->rates.rtmin = upload(net, h.rtmin, rc);
+    net->rates.rtmax = upload(net, h.rtmax, rc);
+    net->rates.flags = upload(net, flags, rc);
+  }
+  // ---- chemistry tables ----
+  const int neq = h.neq;
+  const int E = neq, ONE = neq + 1;
+  std::vector<int2> rab(h.nreac);
+  std::vector<double> nhm(h.nreac);
+  for (int r = 0; r < h.nreac; r++) {
+    int a = h.ra[r], b = (h.ode_kind[r] == ODE_BI) ? h.rb[r] : ONE;
+    if (h.ode_kind[r] == ODE_XRAY) { a = ONE; b = ONE; }
+    rab[r] = make_int2(a == neq ? E : a, b);
+    nhm[r] = (h.ode_kind[r] == ODE_BI || h.ode_kind[r] == ODE_GRAINH2) ? 1.0 : 0.0;
+  }
+  auto terms = stoichiometry(h);
+  if (neq <= kWarp) {
+    WarpTables &w = net->warp;
+    w.neq = neq;
+    w.nreac = h.nreac;
+    const int T = (int)terms.size();
+    w.rhs_len = std::max(1, (T + kWarp - 1) / kWarp);
+    std::vector<int> rr(w.rhs_len * kWarp, 0), fl(w.rhs_len * kWarp, -1);
+    std::vector<double> nu(w.rhs_len * kWarp, 0.0);
+    std::vector<std::vector<int>> parts(kWarp);
+    int slot = 0;
+    for (int l = 0; l < kWarp; l++) {
+      int b = l * w.rhs_len, e = std::min(T, b + w.rhs_len);
+      for (int t = b; t < e; t++) {
+        int k = t - b;
+        rr[k * kWarp + l] = terms[t].r;
+        nu[k * kWarp + l] = terms[t].nu;
+        if (t + 1 == e || terms[t + 1].i != terms[t].i) {
+          fl[k * kWarp + l] = slot;
+          parts[terms[t].i].push_back(slot);
+          slot++;
+        }
+      }
+    }
+    w.nparts = slot;
+    w.plist_len = 1;
+    for (auto &p : parts) w.plist_len = std::max<int>(w.plist_len, (int)p.size());
+    std::vector<int> pl(w.plist_len * kWarp, slot /* zero slot */);
+    for (int i = 0; i < kWarp; i++)
+      for (size_t k = 0; k < parts[i].size(); k++) pl[k * kWarp + i] = parts[i][k];
+    // per-species Jacobian term lists
+    std::vector<std::vector<Term>> per(kWarp);
+    for (auto &t : terms) per[t.i].push_back(t);
+    w.jac_len = 1;
+    for (auto &p : per) w.jac_len = std::max<int>(w.jac_len, (int)p.size());
+    std::vector<int> jr(w.jac_len * kWarp, 0);
+    std::vector<double> jn(w.jac_len * kWarp, 0.0);
+    std::vector<float> jnf(w.jac_len * kWarp, 0.0f);
+    for (int i = 0; i < kWarp; i++)
+      for (size_t k = 0; k < per[i].size(); k++) {
+        jr[k * kWarp + i] = per[i][k].r;
+        jn[k * kWarp + i] = per[i][k].nu;
+        jnf[k * kWarp + i] = (float)per[i][k].nu;
+      }
+    std::vector<double> xe(kWarp, 0.0);
+    for (int i = 0; i < neq; i++) xe[i] = h.xe[i];
+    w.rab = upload(net, rab, rc);
+    w.nh_mask = upload(net, nhm, rc);
+    w.rhs_r = upload(net, rr, rc);
+    w.rhs_nu = upload(net, nu, rc);
+    w.rhs_flush = upload(net, fl, rc);
+    w.plist = upload(net, pl, rc);
+    w.jac_r = upload(net, jr, rc);
+    w.jac_nu = upload(net, jn, rc);
+    w.jac_nu_f = upload(net, jnf, rc);
+    w.xe_coef = upload(net, xe, rc);
+    net->warp_ok = (rc == 0);
+  }
+  return rc;
+}
+
+}  // namespace pdr

@@ -1,0 +1,135 @@
+/*
+ * pdrgpu.h -- C ABI of lib3dpdr_gb300.so, a GB300 (sm_103a) drop-in for the
+ * per-grid-point chemistry and level-population solves of 3D-PDR.
+ *
+ * Every entry point is plain C: pointers, sizes and a cudaStream_t passed as
+ * void*.  "d_" arguments are device pointers, "h_" host pointers.  All
+ * functions return 0 on success and a negative PDR_E_* code on an API error;
+ * pdr_last_error() returns the message of the last error of the calling thread.
+ * There is no CPU fallback: without a usable GPU every compute call fails with
+ * PDR_E_CUDA.
+ */
+#ifndef PDRGPU_H
+#define PDRGPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PDR_E_ARG -1001    /* invalid argument                         */
+#define PDR_E_IO -1002     /* input file missing or malformed          */
+#define PDR_E_CUDA -1003   /* CUDA runtime error (no device, launch)   */
+#define PDR_E_NET -1004    /* network does not fit a kernel / no match */
+
+/* per-cell integrator status, CVODE's flag values (calculate_abundances.c:221-299) */
+#define PDR_OK 0
+#define PDR_TOO_MUCH_WORK -1
+#define PDR_ERR_FAILURE -3
+#define PDR_CONV_FAILURE -4
+
+#define PDR_FP64 0   /* FP64 Newton matrix, partial-pivot LU (CVDense semantics)     */
+#define PDR_MIXED 1  /* FP32 weight-scaled LU of I-gamma*J, FP64 state/RHS/residual;
+                        cells whose Newton iteration fails are re-solved in FP64     */
+
+typedef struct pdr_net pdr_net;
+typedef struct pdr_coolant pdr_coolant;
+
+/* physics constants of params.dat (input_parameters.F90:19-54) */
+typedef struct {
+  double zeta;          /* ZETA = cosmic-ray rate / 1.3e-17 s^-1                      */
+  double omega;         /* dust albedo                                                */
+  double grain_radius;  /* grain radius as given in params.dat                        */
+  double metallicity;
+  double g2d;           /* gas-to-dust ratio                                          */
+  double v_turb;        /* turbulent velocity, cm/s                                   */
+  int h2form;           /* 1: Cazaux & Tielens H2 formation (-DH2FORM), 0: 3e-18 sqrt(T) */
+  int xlambda_linear;   /* 1: tau(lambda)/tau(V) by linear interpolation (the reference's
+                           START-flag variant, shield.F90:398-401,543); 0: natural spline */
+} pdr_phys;
+
+typedef struct {
+  double reltol;        /* relative_abundance_tolerance (1e-8, 3DPDR.F90:462)        */
+  double abstol;        /* absolute_abundance_tolerance (1e-30, 3DPDR.F90:463)       */
+  double start_time_yr; /* start_time (3DPDR.F90:452)                                 */
+  double end_time_yr;   /* end_time (params.dat), used when d_t_end_yr is NULL       */
+  long mxstep;          /* max internal steps per output interval (1e7, calculate_abundances.c:111) */
+  int precision;        /* PDR_FP64 or PDR_MIXED                                      */
+  int warps_per_block;  /* launch shape (0: autotuned/default)                        */
+  int blocks_per_sm;    /* 0: as many as fit                                          */
+} pdr_chem_opts;
+
+void pdr_chem_opts_default(pdr_chem_opts *opts);
+const char *pdr_last_error(void);
+int pdr_device_info(int *sm_count, int *cc_major, int *cc_minor);
+
+/* ---- networks (read_species.F90:15-194, read_rates.F90:9-95) ----
+ * layout_path: optional slot layout of the reference's generated network code
+ * (data/layout_<net>.d); NULL keeps species-file order and name charges. */
+int pdr_net_load(const char *species_path, const char *rates_path, const char *layout_path,
+                 pdr_net **out);
+void pdr_net_free(pdr_net *net);
+int pdr_net_info(const pdr_net *net, int *nspec, int *nreac, int *neq);
+/* register a network for calculate_abundances_ (matched by nspec/nreac) */
+int pdr_net_register(pdr_net *net);
+
+/* ---- chemistry: batched drop-in for calculate_abundances_ ----
+ * d_abundance[ncell*nspec] (column-major (nspec,ncell), updated in place, the
+ * electron slot receives x_e of the last RHS call), d_rate[ncell*nreac],
+ * d_density[ncell]; d_t_end_yr[ncell] or NULL; d_status[ncell] receives the
+ * CVODE flag of each cell; d_stats[ncell*8] (or NULL) receives nst, nfe, nje,
+ * nsetups, nni, ncfn, netf, fell_back_to_fp64.  Replaces
+ * calculate_abundances.c:124-326 for all cells in one persistent launch. */
+int pdr_chem_solve_batched(const pdr_net *net, int ncell, double *d_abundance,
+                           const double *d_rate, const double *d_density,
+                           const double *d_t_end_yr, const pdr_chem_opts *opts, int *d_status,
+                           int *d_stats, void *stream);
+
+/* Legacy symbol with the reference's exact signature (calculate_abundances.c:64):
+ * host arrays, all arguments by reference (gfortran implicit interface).
+ * Tolerances, times and the electron index are read from the Fortran module
+ * variables the reference binds to C (modules.F90:165-166,383,529-530):
+ * chemistry_module_mp_relative_abundance_tolerance_, ..._absolute_..._,
+ * maincode_module_mp_start_time_, maincode_module_mp_end_time_,
+ * global_module_mp_nelect_.  The network is the registered one whose
+ * (nspec, nreac) match, else species_<net>.d/rates_<net>.d found in
+ * $PDR_NETWORK_DIR or the working directory.  Returns the reference's status
+ * (0, or the last failing CVODE flag) or a PDR_E_* code. */
+int calculate_abundances_(double *abundance, double *rate, double *density, double *temperature,
+                          int *npart, int *nspec, int *nreac);
+/* The same host-buffer call with explicit options instead of the Fortran module
+ * variables; net NULL selects the network as calculate_abundances_ does.
+ * Copies in, solves (pdr_chem_solve_batched), copies out, synchronises. */
+int pdr_calculate_abundances(pdr_net *net, double *abundance, double *rate, double *density,
+                             double *temperature, int npart, int nspec, int nreac,
+                             const pdr_chem_opts *opts);
+
+/* ---- reaction rates: batched CALCULATE_REACTION_RATES (calc_reac_rates.F90:16-401) ----
+ * d_rad_surface, d_AV: [ncell*nrays]; d_column5: [ncell*nrays*5] column
+ * densities of H2, HD, CO, C, S along each ray; d_rate[ncell*nreac] out;
+ * d_status[ncell]: 0, or -(reaction number) of a negative rate (the reference STOPs). */
+int pdr_rates_batched(const pdr_net *net, const pdr_phys *phys, int ncell, int nrays,
+                      const double *d_T, const double *d_Td, const double *d_rad_surface,
+                      const double *d_AV, const double *d_column5, double *d_rate, int *d_status,
+                      void *stream);
+/* special reaction numbers NRGR, NRH2, NRHD, NRCO, NRCI, NRSI (1-based, 0 = absent) */
+int pdr_net_special_reactions(const pdr_net *net, int nr[6]);
+
+/* ---- diagnostics (tests pin the device code against the reference with these) ----
+ * The device network RHS, as the generated f() of odes_<net>.c:26-149 computes
+ * it (mode 0: d_out[nstate*neq], x_e of each state in d_xe), or the analytic
+ * Jacobian including dx_e/dx_j (mode 1: d_out[nstate*neq*neq], row-major
+ * J[i][j] = df_i/dx_j; jacobian_<net>.c is the reference counterpart, without
+ * the x_e chain rule).  d_x[nstate*neq], d_rate[nstate*nreac], d_density[nstate]. */
+int pdr_chem_eval_batched(const pdr_net *net, int nstate, const double *d_x, const double *d_rate,
+                          const double *d_density, int mode, double *d_out, double *d_xe, void *stream);
+/* second derivatives of the shielding splines: XLAMBDA's 30-point table
+ * (shield.F90:543) and COSHIELD's 8x6 grid ([iNCO*6+iNH2], shield.F90:398-401) */
+int pdr_shield_tables(double *xderiv30, double *scoderiv48);
+/* FMA throughput of the current device in TFLOP/s (precision 64 or 32), the
+ * FP64/FP32 roofline denominators reported beside the measured kernels */
+int pdr_probe_fma_tflops(int precision, double *tflops, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
