@@ -37,6 +37,11 @@ int launch_rates(const pdr_net *net, const pdr_phys &ph, int ncell, int nrays, c
 int launch_chem_eval(const pdr_net *net, int nstate, const double *x, const double *rate, const double *dens,
                      double *out, double *xe_out, int mode, cudaStream_t st);
 int upload_shield_tables(int dev);
+int build_coolant_tables(pdr_coolant *c);
+int launch_levpop(const pdr_coolant *c, const LevArgsHost &h, bool mixed, int sm_count, cudaStream_t st);
+int launch_heating(const pdr_net *net, int network, const pdr_phys &ph, int ncell, const double *dens,
+                   const double *Tg, const double *Td, const double *uv, const double *ab, const double *rate,
+                   double *out, cudaStream_t st);
 void shield_tables_host(double *xderiv30, double *scoderiv48);
 
 static thread_local std::string g_err;
@@ -241,6 +246,73 @@ int pdr_chem_eval_batched(const pdr_net *net, int nstate, const double *d_x, con
   }
   if (nstate == 0) return 0;
   return launch_chem_eval(net, nstate, d_x, d_rate, d_density, d_out, d_xe, mode, (cudaStream_t)stream);
+}
+
+int pdr_coolant_load(const char *path, int nlev, int ntemp, pdr_coolant **out) {
+  if (!path || !out || nlev < 2 || nlev > 64 || ntemp < 1) {
+    set_error("pdr_coolant_load: invalid argument (2 <= nlev <= 64)");
+    return PDR_E_ARG;
+  }
+  pdr_coolant *c = new pdr_coolant();
+  std::string err = load_coolant(path, nlev, ntemp, c->host);
+  if (!err.empty()) { set_error(err); delete c; return PDR_E_IO; }
+  int rc = build_coolant_tables(c);
+  if (rc) { pdr_coolant_free(c); return rc; }
+  *out = c;
+  return 0;
+}
+
+void pdr_coolant_free(pdr_coolant *c) {
+  if (!c) return;
+  for (void *p : c->allocations) cudaFree(p);
+  delete c;
+}
+
+int pdr_coolant_info(const pdr_coolant *c, int *nlev, int *nlin) {
+  if (!c) { set_error("pdr_coolant_info: null coolant"); return PDR_E_ARG; }
+  if (nlev) *nlev = c->host.nlev;
+  if (nlin) *nlin = c->host.nlin;
+  return 0;
+}
+
+int pdr_levpop_batched(const pdr_coolant *c, int ncell, int nrays, const double *d_density, const double *d_T,
+                       const double *d_Tdust, const double *d_partner5, const double *d_coolant_density,
+                       const double *d_spop, const double *d_tau, int pseudo1d, double metallicity, double g2d,
+                       int precision, double *d_pop, double *d_cooling, double *d_line, int *d_status,
+                       void *stream) {
+  if (!c || ncell < 0 || nrays < 1 || (pseudo1d && nrays < 7) || !d_density || !d_T || !d_Tdust ||
+      !d_partner5 || !d_coolant_density || !d_spop || !d_tau || !d_pop || !d_cooling ||
+      (precision != PDR_FP64 && precision != PDR_MIXED)) {
+    set_error("pdr_levpop_batched: invalid argument");
+    return PDR_E_ARG;
+  }
+  if (ncell == 0) return 0;
+  int dev = 0, sms = 0;
+  int rc = current_device(&dev, &sms);
+  if (rc) return rc;
+  LevArgsHost h;
+  h.ncell = ncell; h.nrays = nrays; h.pseudo1d = pseudo1d; h.metallicity = metallicity; h.g2d = g2d;
+  h.density = d_density; h.T = d_T; h.Td = d_Tdust; h.partner5 = d_partner5; h.cdens = d_coolant_density;
+  h.spop = d_spop; h.tau = d_tau; h.pop = d_pop; h.cooling = d_cooling; h.line = d_line; h.status = d_status;
+  return launch_levpop(c, h, precision == PDR_MIXED, sms, (cudaStream_t)stream);
+}
+
+int pdr_heating_batched(const pdr_net *net, int network, const pdr_phys *phys, int ncell, const double *d_density,
+                        const double *d_Tgas, const double *d_Tdust, const double *d_uv_field,
+                        const double *d_abundance, const double *d_rate, double *d_heating, void *stream) {
+  if (!net || !phys || ncell < 0 || !d_density || !d_Tgas || !d_Tdust || !d_uv_field || !d_abundance ||
+      !d_rate || !d_heating) {
+    set_error("pdr_heating_batched: invalid argument");
+    return PDR_E_ARG;
+  }
+  if (network != 0 && network != 1) {
+    set_error("pdr_heating_batched: chemical heating is defined for the reduced (0) and full (1) networks "
+              "only (the reference STOPs for mynetwork, sub_calculate_heating.F90:250)");
+    return PDR_E_NET;
+  }
+  if (ncell == 0) return 0;
+  return launch_heating(net, network, *phys, ncell, d_density, d_Tgas, d_Tdust, d_uv_field, d_abundance, d_rate,
+                        d_heating, (cudaStream_t)stream);
 }
 
 // diagnostic export of the shielding spline tables (tests compare them with the oracle)

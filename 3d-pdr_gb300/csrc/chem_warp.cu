@@ -69,7 +69,26 @@ struct WarpShared {
   double tau[QMAX + 2];
   double l[QMAX + 1];
   double tq[6];
+  // coefficients of a uniform step history (xi_j = j), per order 1..5:
+  // l[0..5], tq[1..5] (tq[1], tq[3] as computed when an order change is due)
+  double ul[QMAX + 1][QMAX + 1];
+  double utq[QMAX + 1][6];
 };
+
+// squared-norm form of the step-ratio formula eta = 1/((bias*e)^(1/k) + 1e-6)
+// with e2 = e^2; evaluated in FP32 (a heuristic factor, clamped afterwards)
+__device__ __forceinline__ double eta_of(double e2, float bias, int k) {
+  const float v = powf(bias * bias * (float)e2, 0.5f / (float)k);
+  return 1.0 / ((double)v + ADDON);
+}
+
+// 1/x to double precision: FP32 seed and two Newton steps
+__device__ __forceinline__ double rcp_nr(double x) {
+  double r = (double)__frcp_rn((float)x);
+  r = r * fma(-x, r, 2.0);
+  r = r * fma(-x, r, 2.0);
+  return r;
+}
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -109,7 +128,9 @@ __device__ __forceinline__ bool lu_rows(MT (&m)[N], int lane, int &mystep, MT &i
     const int p = argmax_lane(cand ? fabs(m[k]) : MT(0), cand);
     if (p < 0) return false;
     const MT u = bcast(m[k], p);
-    const MT rinv = MT(1) / u;
+    MT rinv;
+    if constexpr (sizeof(MT) == 8) rinv = __drcp_rn(u);
+    else rinv = __frcp_rn(u);
     if (lane == p) { mystep = k; invd = rinv; }
     const bool upd = (mystep < 0);
     const MT l = m[k] * rinv;
@@ -167,7 +188,8 @@ struct Cell {
   MT invd;
   double wsc, ssc;   // setup-time weight and its inverse (mixed scaling)
   // uniform integrator scalars
-  double tn, h, hscale, hprime, eta, etamax, saved_tq5, gamma, gammap, gamrat, rl1, crate, acnrm;
+  double tn, h, hscale, hprime, eta, etamax, saved_tq5, gamma, gammap, gamrat, gscale, rl1;
+  double crate2, acnrm2;   // squared convergence rate and squared WRMS norm of the correction
   double xe_last, rtol, atol;
   int q, qprime, qwait, jcur;
   long long nst, nstlp, nfe, nje, nsetups, nni, ncfn, netf;
@@ -175,12 +197,13 @@ struct Cell {
 
   __device__ __forceinline__ Cell(const ChemArgs &a, int ln) : A(a), lane(ln) {}
 
-  __device__ __forceinline__ double wrms(double v) const {
+  // squared WRMS norm (sum of squares / n); the tests compare squares, so no sqrt
+  __device__ __forceinline__ double wrms2(double v) const {
     double t = (lane < NSP) ? v * ewt : 0.0;
-    return sqrt(warp_sum(t * t) / NSP);
+    return warp_sum(t * t) * (1.0 / NSP);
   }
 
-  __device__ __forceinline__ void set_ewt() { ewt = (lane < NSP) ? 1.0 / (rtol * fabs(z[0]) + atol) : 0.0; }
+  __device__ __forceinline__ void set_ewt() { ewt = (lane < NSP) ? rcp_nr(rtol * fabs(z[0]) + atol) : 0.0; }
 
   // f(y): returns f_lane, records x_e of this call
   __device__ __forceinline__ double rhs(double yv) {
@@ -282,9 +305,10 @@ struct Cell {
     for (int j = 0; j < NSP; j++) finite &= isfinite(m[j]);
     finite = __all_sync(FULL, finite);
     jcur = 1;
-    crate = 1.0;
+    crate2 = 1.0;
     gammap = gamma;
     gamrat = 1.0;
+    gscale = 1.0;
     nstlp = nst;
     return ok && finite;
   }
@@ -297,26 +321,36 @@ struct Cell {
     } else {
       x = lu_solve_rows<NSP, double>(m, lane, mystep, invd, b);
     }
-    if (gamrat != 1.0) x *= 2.0 / (1.0 + gamrat);
+    x *= gscale;   // 2/(1+gamma/gamma_setup) for a stale gamma, else 1
     return (lane < NSP) ? x : 0.0;
   }
 
+  // Pascal-triangle prediction z <- z P (and its inverse), q-specialised
+  template <int Q, int SIGN>
+  __device__ __forceinline__ void pascal() {
+#pragma unroll
+    for (int k = 1; k <= Q; k++)
+#pragma unroll
+      for (int j = Q; j >= k; j--) z[j - 1] = (SIGN > 0) ? z[j - 1] + z[j] : z[j - 1] - z[j];
+  }
+  template <int SIGN>
+  __device__ __forceinline__ void pascal_q() {
+    switch (q) {
+      case 1: pascal<1, SIGN>(); break;
+      case 2: pascal<2, SIGN>(); break;
+      case 3: pascal<3, SIGN>(); break;
+      case 4: pascal<4, SIGN>(); break;
+      default: pascal<5, SIGN>(); break;
+    }
+  }
   __device__ __forceinline__ void predict() {
     tn += h;
-#pragma unroll
-    for (int k = 1; k <= QMAX; k++)
-#pragma unroll
-      for (int j = QMAX; j >= k; j--)
-        if (k <= q && j <= q) z[j - 1] += z[j];
+    pascal_q<1>();
   }
 
   __device__ __forceinline__ void restore(double saved_t) {
     tn = saved_t;
-#pragma unroll
-    for (int k = 1; k <= QMAX; k++)
-#pragma unroll
-      for (int j = QMAX; j >= k; j--)
-        if (k <= q && j <= q) z[j - 1] -= z[j];
+    pascal_q<-1>();
   }
 
   __device__ __forceinline__ void rescale() {
@@ -386,8 +420,10 @@ struct Cell {
       if (j == q + 1) z[j] = zn1;
   }
 
-  __device__ __forceinline__ void set_coeffs() {
-    double l[QMAX + 1];
+  // Fixed-leading-coefficient BDF coefficients l[0..q] and error constants
+  // tq[1..5] for step h and history tau[1..q] (q+1 for tq[3]).
+  __device__ __forceinline__ static void coeffs(int q, bool order_change_due, double h, const double *tau,
+                                                double *l, double *tq) {
 #pragma unroll
     for (int j = 0; j <= QMAX; j++) l[j] = 0.0;
     l[0] = l[1] = 1.0;
@@ -396,7 +432,7 @@ struct Cell {
 #pragma unroll
       for (int j = 2; j < QMAX; j++) {
         if (j < q) {
-          hsum += ws->tau[j - 1];
+          hsum += tau[j - 1];
           xi_inv = h / hsum;
           a0 -= 1.0 / j;
 #pragma unroll
@@ -406,10 +442,7 @@ struct Cell {
       }
       a0 -= 1.0 / q;
       xistar_inv = -l[1] - a0;
-      double tq1 = 0.0;
-#pragma unroll
-      for (int j = 1; j <= QMAX; j++) if (j == q - 1) tq1 = ws->tau[j];
-      hsum += tq1;
+      hsum += tau[q - 1];
       xi_inv = h / hsum;
       a0hat = -l[1] - xi_inv;
 #pragma unroll
@@ -420,45 +453,83 @@ struct Cell {
 #pragma unroll
     for (int j = 0; j <= QMAX; j++) if (j == q) lq = l[j];
     const double A1 = 1.0 - a0hat + a0, A2 = 1.0 + q * A1;
-    double tq[6];
-    tq[1] = ws->tq[1];
-    tq[3] = ws->tq[3];
     tq[2] = fabs(A1 / (a0 * A2));
     tq[5] = fabs(A2 * xistar_inv / (lq * xi_inv));
-    if (qwait == 1) {
+    if (order_change_due) {
       if (q > 1) {
         const double C = xistar_inv / lq, A3 = a0 + 1.0 / q, A4 = a0hat + xi_inv;
         tq[1] = fabs(C * (1.0 - A4 + A3) / A3);
       } else {
         tq[1] = 1.0;
       }
-      double tqq = 0.0;
-#pragma unroll
-      for (int j = 1; j <= QMAX; j++) if (j == q) tqq = ws->tau[j];
-      hsum += tqq;
+      hsum += tau[q];
       xi_inv = h / hsum;
       const double A5 = a0 - 1.0 / (q + 1), A6 = a0hat - xi_inv;
       tq[3] = fabs(((1.0 - A6 + A5) / A2) / (xi_inv * (q + 2) * A5));
     }
     tq[4] = NLSCOEF / tq[2];
-    __syncwarp();
-    if (lane == 0) {
+  }
+
+  // the per-warp table of uniform-history coefficients (h = tau_j = 1)
+  __device__ __forceinline__ void build_uniform_table() {
+    double one[QMAX + 2];
 #pragma unroll
-      for (int j = 0; j <= QMAX; j++) ws->l[j] = l[j];
-      ws->tq[1] = tq[1]; ws->tq[2] = tq[2]; ws->tq[3] = tq[3]; ws->tq[4] = tq[4]; ws->tq[5] = tq[5];
+    for (int j = 0; j < QMAX + 2; j++) one[j] = 1.0;
+    for (int qq = 1; qq <= QMAX; qq++) {
+      double l[QMAX + 1], tq[6];
+      coeffs(qq, true, 1.0, one, l, tq);
+      __syncwarp();
+      if (lane == 0) {
+        for (int j = 0; j <= QMAX; j++) ws->ul[qq][j] = l[j];
+        for (int j = 1; j <= 5; j++) ws->utq[qq][j] = tq[j];
+      }
     }
     __syncwarp();
-    rl1 = 1.0 / l[1];
+  }
+
+  __device__ __forceinline__ void set_coeffs() {
+    // a history of equal steps gives xi_j = j exactly: take the tabulated values
+    bool uniform = true;
+#pragma unroll
+    for (int j = 1; j <= QMAX; j++)
+      if (j <= q && ws->tau[j] != h) uniform = false;
+    __syncwarp();
+    if (uniform) {
+      if (lane == 0) {
+#pragma unroll
+        for (int j = 0; j <= QMAX; j++) ws->l[j] = ws->ul[q][j];
+        ws->tq[2] = ws->utq[q][2];
+        ws->tq[4] = ws->utq[q][4];
+        ws->tq[5] = ws->utq[q][5];
+        if (qwait == 1) { ws->tq[1] = ws->utq[q][1]; ws->tq[3] = ws->utq[q][3]; }
+      }
+    } else {
+      double l[QMAX + 1], tq[6];
+      tq[1] = ws->tq[1];
+      tq[3] = ws->tq[3];
+      coeffs(q, qwait == 1, h, ws->tau, l, tq);
+      if (lane == 0) {
+#pragma unroll
+        for (int j = 0; j <= QMAX; j++) ws->l[j] = l[j];
+        ws->tq[1] = tq[1]; ws->tq[2] = tq[2]; ws->tq[3] = tq[3]; ws->tq[4] = tq[4]; ws->tq[5] = tq[5];
+      }
+    }
+    __syncwarp();
+    rl1 = 1.0 / ws->l[1];
     gamma = h * rl1;
     if (nst == 0) gammap = gamma;
     gamrat = (nst > 0) ? gamma / gammap : 1.0;
+    gscale = (gamrat != 1.0) ? 2.0 / (1.0 + gamrat) : 1.0;
   }
 
   // 0 solved, 1 convergence failure (recoverable), 2 convergence failure that
-  // sends a mixed-precision cell to the FP64 pass
+  // sends a mixed-precision cell to the FP64 pass.  Norms are kept squared:
+  // the tests del*min(1,R) <= 0.1/C_err, del > 2 del_prev and R = max(0.3 R,
+  // del/del_prev) are evaluated on squares.
   __device__ __forceinline__ int nls(bool prev_fail) {
     bool call_setup = prev_fail || (nst == 0) || (nst >= nstlp + MSBP) || (fabs(gamrat - 1.0) > DGMAX);
     const double tq4 = ws->tq[4];
+    const double tq4sq = tq4 * tq4;
     for (int attempt = 0; attempt < 2; attempt++) {
       y = z[0];
       ftmp = rhs(y);
@@ -467,27 +538,26 @@ struct Cell {
         call_setup = false;
       }
       acor = 0.0;
-      double delp = 0.0;
+      double delp2 = 0.0;
       int mcor = 0;
       bool conv = false;
       for (;;) {
         tmp = gamma * ftmp - (rl1 * z[1] + acor);
         tmp = solve(tmp);
         nni++;
-        const double del = wrms(tmp);
+        const double del2 = wrms2(tmp);
         acor += tmp;
         y = z[0] + acor;
-        if (mcor > 0) crate = fmax(CRDOWN * crate, del / delp);
-        const double dcon = del * fmin(1.0, crate) / tq4;
-        if (dcon <= 1.0) {
-          acnrm = (mcor == 0) ? del : wrms(acor);
+        if (mcor > 0) crate2 = fmax(CRDOWN * CRDOWN * crate2, del2 / delp2);
+        if (del2 * fmin(1.0, crate2) <= tq4sq) {
+          acnrm2 = (mcor == 0) ? del2 : wrms2(acor);
           jcur = 0;
           conv = true;
           break;
         }
         mcor++;
-        if (mcor == MAXCOR || (mcor >= 2 && del > RDIV * delp)) break;
-        delp = del;
+        if (mcor == MAXCOR || (mcor >= 2 && del2 > RDIV * RDIV * delp2)) break;
+        delp2 = del2;
         ftmp = rhs(y);
       }
       if (conv) return 0;
@@ -507,7 +577,7 @@ struct Cell {
     const double saved_t = tn;
     int ncf = 0, nef = 0;
     bool prev_fail = false;
-    double dsm = 0.0;
+    double dsm2 = 0.0;
     if (nst > 0 && hprime != h) {
       if (qprime != q) {
         if (qprime > q) increase_order();
@@ -533,8 +603,9 @@ struct Cell {
         rescale();
         continue;
       }
-      dsm = acnrm * ws->tq[2];
-      if (dsm <= 1.0) break;
+      const double tq2 = ws->tq[2];
+      dsm2 = acnrm2 * (tq2 * tq2);
+      if (dsm2 <= 1.0) break;
       nef++;
       netf++;
       prev_fail = true;
@@ -543,7 +614,7 @@ struct Cell {
       etamax = 1.0;
       const int L = q + 1;
       if (nef <= MXNEF1) {
-        eta = 1.0 / (pow(BIAS2 * dsm, 1.0 / L) + ADDON);
+        eta = eta_of(dsm2, (float)BIAS2, L);
         eta = fmax(ETAMIN, eta);
         if (nef >= SMALL_NEF) eta = fmin(eta, ETAMXF);
         rescale();
@@ -575,9 +646,11 @@ struct Cell {
       ws->tau[1] = h;
     }
     __syncwarp();
-#pragma unroll
-    for (int j = 0; j <= QMAX; j++)
-      if (j <= q) z[j] = fma(ws->l[j], acor, z[j]);
+    switch (q) {
+#define PDR_CORRECT(Q) case Q: _Pragma("unroll") for (int j = 0; j <= Q; j++) z[j] = fma(ws->l[j], acor, z[j]); break;
+      PDR_CORRECT(1) PDR_CORRECT(2) PDR_CORRECT(3) PDR_CORRECT(4) PDR_CORRECT(5)
+#undef PDR_CORRECT
+    }
     qwait--;
     if (qwait == 1 && q != QMAX) {
       z[QMAX] = acor;
@@ -590,7 +663,7 @@ struct Cell {
       eta = 1.0;
     } else {
       const int L = q + 1;
-      const double etaq = 1.0 / (pow(BIAS2 * dsm, 1.0 / L) + ADDON);
+      const double etaq = eta_of(dsm2, (float)BIAS2, L);
       if (qwait != 0) {
         eta = etaq;
         qprime = q;
@@ -602,13 +675,16 @@ struct Cell {
           double zq = 0.0;
 #pragma unroll
           for (int j = 0; j <= QMAX; j++) if (j == q) zq = z[j];
-          const double ddn = wrms(zq) * ws->tq[1];
-          etaqm1 = 1.0 / (pow(BIAS1 * ddn, 1.0 / q) + ADDON);
+          const double tq1 = ws->tq[1];
+          etaqm1 = eta_of(wrms2(zq) * (tq1 * tq1), (float)BIAS1, q);
         }
         if (q != QMAX && saved_tq5 != 0.0) {
-          const double cquot = (ws->tq[5] / saved_tq5) * pow(h / ws->tau[2], (double)L);
-          const double dup = wrms(acor - cquot * z[QMAX]) * ws->tq[3];
-          etaqp1 = 1.0 / (pow(BIAS3 * dup, 1.0 / (L + 1)) + ADDON);
+          const double ratio = h / ws->tau[2];
+          double rp = ratio;
+          for (int k = 1; k < L; k++) rp *= ratio;
+          const double cquot = (ws->tq[5] / saved_tq5) * rp;
+          const double tq3 = ws->tq[3];
+          etaqp1 = eta_of(wrms2(acor - cquot * z[QMAX]) * (tq3 * tq3), (float)BIAS3, L + 1);
         }
         const double etam = fmax(etaqm1, fmax(etaq, etaqp1));
         if (etam < THRESH) { eta = 1.0; qprime = q; }
@@ -637,7 +713,7 @@ struct Cell {
     double hnew = hg;
     for (int it = 1; it <= 4; it++) {
       tmp = rhs(z[0] + hg * z[1]);
-      const double yddnrm = wrms((tmp - z[1]) / hg);
+      const double yddnrm = sqrt(wrms2((tmp - z[1]) / hg));
       if (ok || it == 4) { hnew = hg; break; }
       hnew = (yddnrm * hub * hub > 2.0) ? sqrt(2.0 / yddnrm) : sqrt(hg * hub);
       const double hrat = hnew / hg;
@@ -714,9 +790,10 @@ struct Cell {
     nfe = nje = nsetups = nni = ncfn = netf = 0;
     nst = nstlp = 0;
     saved_tq5 = 0.0;
-    crate = 1.0;
+    crate2 = 1.0;
     gammap = gamma = 1.0;
     gamrat = 1.0;
+    gscale = 1.0;
     jcur = 0;
     acor = 0.0;
     const double t0 = A.start_time_yr * YEAR;
@@ -770,7 +847,7 @@ struct Cell {
 };
 
 template <int NSP, bool MIXED>
-__global__ void __launch_bounds__(256) chem_warp_kernel(const __grid_constant__ ChemArgs A, int total_cells, const int *total_ptr) {
+__global__ void __launch_bounds__(256, 1) chem_warp_kernel(const __grid_constant__ ChemArgs A, int total_cells, const int *total_ptr) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   using MT = typename std::conditional<MIXED, float, double>::type;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -791,6 +868,7 @@ __global__ void __launch_bounds__(256) chem_warp_kernel(const __grid_constant__ 
   c.jrow = reinterpret_cast<MT *>(base + al(kn_b) + al(scr_b) + al(xs_b) + al(part_b));
   c.sig = reinterpret_cast<float *>(base + al(kn_b) + al(scr_b) + al(xs_b) + al(part_b) + al(jrow_b));
   c.ws = reinterpret_cast<WarpShared *>(base + al(kn_b) + al(scr_b) + al(xs_b) + al(part_b) + al(jrow_b) + al(sig_b));
+  c.build_uniform_table();
   if (total_ptr) total_cells = *total_ptr;
   for (;;) {
     int idx = 0;

@@ -1,0 +1,321 @@
+// levpop.cu -- batched statistical-equilibrium solves for one coolant
+// (the per-cell, per-coolant step of 3DPDR.F90:756-843: FIND_CCOEFF,
+// escape_probability after the optical depths are known, solvlevpop).
+//
+// One warp per cell.  The lanes share the nlev x nlev work:
+//   C_ij   linear-in-T interpolation of each partner's table, partners summed in
+//          LAMDA-id order with the para/ortho split (find_Ccoeff.F90:35-147);
+//   field  per radiative pair: CMB + dust Planck background, source function,
+//          ray-averaged escape probability beta(tau) with the masing and
+//          small-tau guards (escape_probability.F90:51-167; PSEUDO_1D uses ray 6);
+//   R_ij = A_ij + B_ij <J_ij> + C_ij (|R| < 1e-50 -> 0);
+//   the solvlevpop matrix (transposed rates, diagonal = -row sum, last row
+//   1e-8, rhs = density*1e-8, solvlevpop.F90:18-35) held in shared memory and
+//   solved either in FP64 by the reference's Gauss-Jordan elimination with full
+//   pivoting (same pivot order, unfused products as in the reference), or by
+//   FP32 Gauss-Jordan giving an approximate inverse plus one FP64
+//   iterative-refinement step; negative populations are set to zero.
+#include "pdr_internal.h"
+
+namespace pdr {
+namespace {
+
+constexpr double KB = 1.38065040e-16, CL = 2.99792458e+10, HP = 6.62606896e-27;
+constexpr double PI = 3.141592653589793238462643383279502884197;
+constexpr unsigned FULL = 0xffffffffu;
+
+struct LevArgs {
+  int ncell, nrays, pseudo1d;
+  double metallicity, g2d;
+  const double *density, *T, *Td, *partner5, *cdens, *spop, *tau;
+  double *pop, *cooling, *line;
+  int *status;
+};
+
+// warp argmax of (value, index) with ties resolved to the larger index
+__device__ __forceinline__ void argmax_last(double &v, int &idx) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const double ov = __shfl_xor_sync(FULL, v, o);
+    const int oi = __shfl_xor_sync(FULL, idx, o);
+    if (ov > v || (ov == v && oi > idx)) { v = ov; idx = oi; }
+  }
+}
+
+// Gauss-Jordan with full pivoting on a (n x n, row stride n) and one rhs b,
+// warp-cooperative; the pivot search reproduces the serial scan's choice
+// (last maximum in row-major order).  Returns false on a singular matrix.
+template <class R>
+__device__ bool gauss_jordan(R *a, R *b, int n, int *ipiv, int *indxr, int *indxc, bool unscramble) {
+  const int lane = threadIdx.x & 31;
+  for (int j = lane; j < n; j += 32) ipiv[j] = 0;
+  __syncwarp();
+  for (int it = 0; it < n; it++) {
+    double best = -1.0;
+    int bidx = -1;
+    for (int e = lane; e < n * n; e += 32) {
+      const int j = e / n, k = e - j * n;
+      if (ipiv[j] != 1 && ipiv[k] == 0) {
+        const double v = fabs((double)a[e]);
+        if (v >= best) { best = v; bidx = e; }
+      }
+    }
+    argmax_last(best, bidx);
+    if (bidx < 0) return false;
+    const int irow = bidx / n, icol = bidx - irow * n;
+    __syncwarp();
+    if (lane == 0) ipiv[icol]++;
+    if (irow != icol) {
+      for (int l = lane; l < n; l += 32) {
+        const R d = a[irow * n + l];
+        a[irow * n + l] = a[icol * n + l];
+        a[icol * n + l] = d;
+      }
+      if (lane == 0) { const R d = b[irow]; b[irow] = b[icol]; b[icol] = d; }
+    }
+    if (lane == 0) { indxr[it] = irow; indxc[it] = icol; }
+    __syncwarp();
+    const R piv = a[icol * n + icol];
+    if (piv == R(0)) return false;
+    const R pivinv = R(1) / piv;
+    __syncwarp();
+    if (lane == 0) a[icol * n + icol] = R(1);
+    __syncwarp();
+    for (int l = lane; l < n; l += 32) a[icol * n + l] = a[icol * n + l] * pivinv;
+    if (lane == 0) b[icol] = b[icol] * pivinv;
+    __syncwarp();
+    for (int ll = lane; ll < n; ll += 32) {
+      if (ll == icol) continue;
+      const R dum = a[ll * n + icol];
+      a[ll * n + icol] = R(0);
+      for (int l = 0; l < n; l++) {
+        if constexpr (sizeof(R) == 8) a[ll * n + l] = __dsub_rn(a[ll * n + l], __dmul_rn(a[icol * n + l], dum));
+        else a[ll * n + l] = __fsub_rn(a[ll * n + l], __fmul_rn(a[icol * n + l], dum));
+      }
+      if constexpr (sizeof(R) == 8) b[ll] = __dsub_rn(b[ll], __dmul_rn(b[icol], dum));
+      else b[ll] = __fsub_rn(b[ll], __fmul_rn(b[icol], dum));
+    }
+    __syncwarp();
+  }
+  if (unscramble) {
+    for (int l = n - 1; l >= 0; l--) {
+      const int r = indxr[l], c = indxc[l];
+      if (r != c)
+        for (int k = lane; k < n; k += 32) {
+          const R d = a[k * n + r];
+          a[k * n + r] = a[k * n + c];
+          a[k * n + c] = d;
+        }
+      __syncwarp();
+    }
+  }
+  return true;
+}
+
+template <bool MIXED>
+__global__ void __launch_bounds__(256) levpop_kernel(const __grid_constant__ CoolantTables C,
+                                                     const __grid_constant__ LevArgs A) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int n = C.nlev, nn = n * n;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  auto al = [](size_t v) { return (v + 15) & ~size_t(15); };
+  const size_t per_warp = al(8 * nn) * 2 + al(8 * n) * 3 + al(4 * n) * 3;
+  unsigned char *base = smem + per_warp * warp;
+  double *R = reinterpret_cast<double *>(base);              // rates, then the solvlevpop matrix
+  double *aux = reinterpret_cast<double *>(base + al(8 * nn)); // line values, then FP32 matrix
+  double *b = reinterpret_cast<double *>(base + 2 * al(8 * nn));
+  double *sp = b + al(8 * n) / 8;
+  double *x = sp + al(8 * n) / 8;
+  int *ipiv = reinterpret_cast<int *>(reinterpret_cast<unsigned char *>(x) + al(8 * n));
+  int *indxr = ipiv + al(4 * n) / 4;
+  int *indxc = indxr + al(4 * n) / 4;
+  const int wpb = blockDim.x >> 5;
+  for (int cell = blockIdx.x * wpb + warp; cell < A.ncell; cell += gridDim.x * wpb) {
+    const double T = A.T[cell], Td = A.Td[cell], rho = A.density[cell];
+    const double *p5 = A.partner5 + (size_t)cell * 5;
+    const double nH = p5[0], nHp = p5[1], ne = p5[2], nHe = p5[3], nH2 = p5[4];
+    for (int i = lane; i < n; i += 32) sp[i] = A.spop[(size_t)cell * n + i];
+    // ---- collision rates ----
+    double fpara = 0.0, fortho = 0.0;
+    if (nH2 > 0.0) { fpara = 1.0 / (1.0 + 9.0 * exp(-170.5 / T)); fortho = 1.0 - fpara; }
+    for (int e = lane; e < nn; e += 32) R[e] = 0.0;
+    __syncwarp();
+    for (int q = 0; q < C.npart; q++) {
+      const int p = C.part[q];
+      const double *tp = C.temps + (size_t)q * C.ntemp;
+      int klo = 0, khi = 0;
+      for (int k = 1; k <= C.ntemp; k++) {
+        if (tp[k - 1] > T) { klo = k - 1; khi = k; break; }
+        else if (tp[k - 1] == 0.0) { klo = k - 1; khi = k - 1; break; }
+      }
+      if (khi == 0) { klo = C.ntemp; khi = C.ntemp; }
+      else if (khi == 1) { klo = 1; khi = 1; }
+      const double step = (klo == khi) ? 0.0 : (T - tp[klo - 1]) / (tp[khi - 1] - tp[klo - 1]);
+      const double *lo = C.col + ((size_t)q * C.ntemp + (klo - 1)) * nn;
+      const double *hi = C.col + ((size_t)q * C.ntemp + (khi - 1)) * nn;
+      for (int e = lane; e < nn; e += 32) {
+        const double tmp = lo[e] + (hi[e] - lo[e]) * step;
+        double add;
+        if (p == 1) add = tmp * nH2 * fpara;
+        else if (p == 2) add = tmp * nH2 * fortho;
+        else add = tmp * (p == 0 ? nH2 : p == 3 ? ne : p == 4 ? nH : p == 5 ? nHe : nHp);
+        R[e] = R[e] + add;
+      }
+    }
+    __syncwarp();
+    // ---- escape probabilities and the radiative terms ----
+    const double ngrain = 2.0e-12 * rho * A.metallicity * 100. / A.g2d;
+    const double *tau = A.tau + (size_t)cell * C.nlin * A.nrays;
+    for (int e = lane; e < nn; e += 32) {
+      const int i = e / n, j = e - i * n;
+      aux[e] = 0.0;
+      if (j >= i) continue;
+      const double f = C.freq[e], Aij = C.A[e];
+      const double tmp2 = 2.0 * HP * (f * f * f) / (CL * CL);
+      double bb = tmp2 * (1.0 / (exp(HP * f / KB / 2.7) - 1.0));
+      const double emis = (2.0 * ngrain) * ((double)0.01f * ((double)1.3f * f / 3.0e11));
+      bb = bb + tmp2 * (1.0 / (exp(HP * f / KB / Td) - 1.0) * emis);
+      double S, beta;
+      bool has_line = true;
+      if (sp[i] == 0.0) {
+        S = 0.0; beta = 1.0; has_line = false;
+      } else {
+        const double tpop = (sp[j] * C.weights[i]) / (sp[i] * C.weights[j]) - 1.0;
+        if (fabs(tpop) < 1.0e-50) {
+          S = HP * f * sp[i] * Aij / 4. / PI;
+          beta = 1.0;
+        } else {
+          S = tmp2 / tpop;
+          const int li = C.line_of_pair[e];
+          double bsum = 0.0;
+          for (int r = 0; r < A.nrays; r++) {
+            double t = (A.pseudo1d && r != 6) ? 1.0e50 : (li >= 0 ? tau[li * A.nrays + r] : 0.0);
+            double br;
+            if (t < -5.0) br = (1.0 - exp(5.0)) / (-5.0);
+            else if (fabs(t) < 1.0e-8) br = 1.0;
+            else br = (1.0 - exp(-t)) / t;
+            bsum += br;
+          }
+          beta = A.pseudo1d ? bsum : bsum / (double)A.nrays;
+        }
+      }
+      if (has_line) aux[e] = Aij * HP * f * sp[i] * beta * (S - bb) / S;
+      const double field = (1.0 - beta) * S + beta * bb;
+      const int et = j * n + i;
+      R[e] = (Aij + C.B[e] * field) + R[e];
+      R[et] = (C.A[et] + C.B[et] * field) + R[et];
+    }
+    __syncwarp();
+    for (int e = lane; e < nn; e += 32)
+      if (fabs(R[e]) < 1.0e-50) R[e] = 0.0;
+    __syncwarp();
+    if (lane == 0) {
+      double cool = 0.0;
+      for (int i = 0; i < n; i++)
+        for (int j = 0; j < i; j++) cool = cool + aux[i * n + j];
+      A.cooling[cell] = cool;
+    }
+    if (A.line)
+      for (int e = lane; e < nn; e += 32) A.line[(size_t)cell * nn + e] = aux[e];
+    // ---- solvlevpop matrix: transpose, diagonal -sum, conservation row ----
+    for (int i = lane; i < n; i += 32) {
+      double out = 0.0;
+      for (int j = 0; j < n; j++) out = out + R[i * n + j];
+      b[i] = out;
+    }
+    __syncwarp();
+    for (int e = lane; e < nn; e += 32) {
+      const int i = e / n, j = e - i * n;
+      if (j > i) { const double t = R[e]; R[e] = R[j * n + i]; R[j * n + i] = t; }
+    }
+    __syncwarp();
+    for (int i = lane; i < n; i += 32) R[i * n + i] = -b[i];
+    __syncwarp();
+    for (int i = lane; i < n; i += 32) { R[(n - 1) * n + i] = 1.0e-8; b[i] = 0.0; }
+    __syncwarp();
+    const double dens = A.cdens[cell];
+    if (lane == 0) b[n - 1] = dens * 1.0e-8;
+    __syncwarp();
+    bool ok;
+    if constexpr (!MIXED) {
+      ok = gauss_jordan<double>(R, b, n, ipiv, indxr, indxc, false);
+      for (int i = lane; i < n; i += 32) x[i] = b[i];
+    } else {
+      float *Mf = reinterpret_cast<float *>(aux);
+      float *bf = Mf + nn;
+      for (int e = lane; e < nn; e += 32) Mf[e] = (float)R[e];
+      for (int i = lane; i < n; i += 32) bf[i] = 0.0f;
+      __syncwarp();
+      ok = gauss_jordan<float>(Mf, bf, n, ipiv, indxr, indxc, true);   // Mf := approximate inverse
+      __syncwarp();
+      // x0 = inv b ; r = b - M x0 (FP64) ; x = x0 + inv r
+      for (int i = lane; i < n; i += 32) {
+        double s = 0.0;
+        for (int l = 0; l < n; l++) s = fma((double)Mf[i * n + l], b[l], s);
+        x[i] = s;
+      }
+      __syncwarp();
+      for (int i = lane; i < n; i += 32) {
+        double s = b[i];
+        for (int l = 0; l < n; l++) s = fma(-R[i * n + l], x[l], s);
+        sp[i] = s;   // residual (s_pop no longer needed)
+      }
+      __syncwarp();
+      for (int i = lane; i < n; i += 32) {
+        double s = 0.0;
+        for (int l = 0; l < n; l++) s = fma((double)Mf[i * n + l], sp[l], s);
+        x[i] += s;
+      }
+    }
+    __syncwarp();
+    for (int i = lane; i < n; i += 32) {
+      double v = x[i];
+      if (v < 0.0) v = 0.0;
+      A.pop[(size_t)cell * n + i] = v;
+    }
+    if (lane == 0 && A.status) A.status[cell] = ok ? 0 : 1;
+    __syncwarp();
+  }
+}
+
+}  // namespace
+
+size_t levpop_smem_per_warp(int n) {
+  auto al = [](size_t v) { return (v + 15) & ~size_t(15); };
+  return al(8 * (size_t)n * n) * 2 + al(8 * n) * 3 + al(4 * n) * 3;
+}
+
+int launch_levpop(const pdr_coolant *c, const LevArgsHost &h, bool mixed, int sm_count, cudaStream_t st) {
+  LevArgs A;
+  A.ncell = h.ncell; A.nrays = h.nrays; A.pseudo1d = h.pseudo1d;
+  A.metallicity = h.metallicity; A.g2d = h.g2d;
+  A.density = h.density; A.T = h.T; A.Td = h.Td; A.partner5 = h.partner5; A.cdens = h.cdens;
+  A.spop = h.spop; A.tau = h.tau; A.pop = h.pop; A.cooling = h.cooling; A.line = h.line; A.status = h.status;
+  const int n = c->dev.nlev;
+  const size_t pw = levpop_smem_per_warp(n);
+  int wpb = (int)((96 * 1024) / pw);
+  if (wpb > 8) wpb = 8;
+  if (wpb < 1) wpb = 1;
+  const size_t smem = pw * wpb;
+  cudaError_t e;
+  int per_sm = 0;
+  if (mixed) {
+    e = cudaFuncSetAttribute(levpop_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(levpop)");
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, levpop_kernel<true>, wpb * 32, smem);
+  } else {
+    e = cudaFuncSetAttribute(levpop_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(levpop)");
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, levpop_kernel<false>, wpb * 32, smem);
+  }
+  if (per_sm < 1) per_sm = 1;
+  long long blocks = ((long long)h.ncell + wpb - 1) / wpb;
+  if (blocks > (long long)sm_count * per_sm) blocks = (long long)sm_count * per_sm;
+  if (blocks < 1) blocks = 1;
+  if (mixed) levpop_kernel<true><<<(int)blocks, wpb * 32, smem, st>>>(c->dev, A);
+  else levpop_kernel<false><<<(int)blocks, wpb * 32, smem, st>>>(c->dev, A);
+  e = cudaGetLastError();
+  return e == cudaSuccess ? 0 : cuda_fail(e, "levpop_kernel launch");
+}
+
+}  // namespace pdr

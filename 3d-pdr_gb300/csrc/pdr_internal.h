@@ -70,7 +70,41 @@ struct HostNet {
 
 std::string load_network(const char *species, const char *rates, const char *layout, HostNet &net);
 
+// A LAMDA coolant as read by read_input.F90 (element (i,j) at i*nlev+j, 0-based)
+struct HostCoolant {
+  int nlev = 0, ntemp = 0, nlin = 0;
+  std::vector<double> energies, weights, A, B, freq, temps /*[7][ntemp]*/, col /*[7][nlev*nlev][ntemp]*/;
+  std::vector<int> line_up, line_lo;
+};
+std::string load_coolant(const char *path, int nlev, int ntemp, HostCoolant &c);
+
+// Device tables of one coolant for the level-population kernel
+struct CoolantTables {
+  int nlev = 0, ntemp = 0, nlin = 0, npart = 0;
+  int part[7] = {0, 0, 0, 0, 0, 0, 0};   // LAMDA partner ids (0-based) with rates, ascending
+  double *temps = nullptr;     // [npart][ntemp]
+  double *col = nullptr;       // [npart][ntemp][nlev*nlev]
+  double *A = nullptr, *B = nullptr, *freq = nullptr, *weights = nullptr;
+  int *line_of_pair = nullptr; // [nlev*nlev] radiative line of (i,j), i>j, else -1
+};
+
+// host-side argument bundle of the level-population launch
+struct LevArgsHost {
+  int ncell = 0, nrays = 0, pseudo1d = 0;
+  double metallicity = 1.0, g2d = 100.0;
+  const double *density = nullptr, *T = nullptr, *Td = nullptr, *partner5 = nullptr, *cdens = nullptr,
+               *spop = nullptr, *tau = nullptr;
+  double *pop = nullptr, *cooling = nullptr, *line = nullptr;
+  int *status = nullptr;
+};
+
 }  // namespace pdr
+
+struct pdr_coolant {
+  pdr::HostCoolant host;
+  pdr::CoolantTables dev;
+  std::vector<void *> allocations;
+};
 
 struct pdr_net {
   pdr::HostNet host;

@@ -68,6 +68,12 @@ def lib():
     L.pdr_calculate_abundances.argtypes = [_vp, _vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_int,
                                            C.POINTER(ChemOpts)]
     L.pdr_probe_fma_tflops.argtypes = [C.c_int, C.POINTER(C.c_double), _vp]
+    L.pdr_heating_batched.argtypes = [_vp, C.c_int, C.POINTER(Phys), C.c_int] + [_vp] * 8
+    L.pdr_coolant_load.argtypes = [C.c_char_p, C.c_int, C.c_int, C.POINTER(_vp)]
+    L.pdr_coolant_free.argtypes = [_vp]
+    L.pdr_coolant_info.argtypes = [_vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    L.pdr_levpop_batched.argtypes = [_vp, C.c_int, C.c_int] + [_vp] * 7 + [C.c_int, C.c_double, C.c_double,
+                                                                          C.c_int] + [_vp] * 5
     _LIB = L
     return L
 
@@ -223,3 +229,56 @@ def probe_fma_tflops(precision=64, stream=None):
     v = C.c_double()
     check(lib().pdr_probe_fma_tflops(precision, C.byref(v), _stream(stream)), "pdr_probe_fma_tflops")
     return v.value
+
+
+# LAMDA files and array capacities of the four coolants (input_parameters.F90:120-127)
+COOLANTS = {"CII": ("12c+.dat", 5, 18), "CI": ("12c.dat", 5, 29), "OI": ("16o.dat", 5, 27),
+            "CO": ("12co.dat", 41, 25)}
+
+
+class Coolant:
+    """A coolant's level/collision data on the device (read_input.F90)."""
+
+    def __init__(self, key, data_dir=DATA):
+        fname, nlev, ntemp = COOLANTS[key]
+        h = _vp()
+        check(lib().pdr_coolant_load(os.path.join(data_dir, fname).encode(), nlev, ntemp, C.byref(h)),
+              "pdr_coolant_load")
+        self.handle, self.key = h, key
+        a, b = C.c_int(), C.c_int()
+        check(lib().pdr_coolant_info(h, C.byref(a), C.byref(b)), "pdr_coolant_info")
+        self.nlev, self.nlin = a.value, b.value
+
+    def close(self):
+        if getattr(self, "handle", None) is not None and _LIB is not None:
+            _LIB.pdr_coolant_free(self.handle)
+            self.handle = None
+
+
+def level_populations(cool, density, T, Tdust, partner5, coolant_density, spop, tau, pseudo1d=False,
+                      metallicity=1.0, g2d=100.0, precision="fp64", want_line=False, stream=None):
+    """Batched level-population step of one coolant; tau (ncell, nlin, nrays).
+    Returns (pop, cooling, line or None, status)."""
+    import torch
+    ncell, nrays = density.shape[0], tau.shape[-1]
+    dev = density.device
+    pop = torch.empty((ncell, cool.nlev), dtype=torch.float64, device=dev)
+    cooling = torch.empty(ncell, dtype=torch.float64, device=dev)
+    line = torch.empty((ncell, cool.nlev, cool.nlev), dtype=torch.float64, device=dev) if want_line else None
+    status = torch.empty(ncell, dtype=torch.int32, device=dev)
+    check(lib().pdr_levpop_batched(cool.handle, ncell, nrays, _ptr(density), _ptr(T), _ptr(Tdust),
+                                   _ptr(partner5), _ptr(coolant_density), _ptr(spop), _ptr(tau),
+                                   1 if pseudo1d else 0, metallicity, g2d,
+                                   PDR_MIXED if precision == "mixed" else PDR_FP64, _ptr(pop), _ptr(cooling),
+                                   _ptr(line), _ptr(status), _stream(stream)), "pdr_levpop_batched")
+    return pop, cooling, line, status
+
+
+def heating(net, network, ph, density, Tgas, Tdust, uv_field, abundance, rate, stream=None):
+    """Batched CALC_HEATING; network 0 reduced / 1 full.  Returns (ncell, 12)."""
+    import torch
+    out = torch.empty((density.shape[0], 12), dtype=torch.float64, device=density.device)
+    check(lib().pdr_heating_batched(net.handle, network, C.byref(ph), density.shape[0], _ptr(density),
+                                    _ptr(Tgas), _ptr(Tdust), _ptr(uv_field), _ptr(abundance), _ptr(rate),
+                                    _ptr(out), _stream(stream)), "pdr_heating_batched")
+    return out

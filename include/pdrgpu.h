@@ -114,6 +114,42 @@ int pdr_rates_batched(const pdr_net *net, const pdr_phys *phys, int ncell, int n
 /* special reaction numbers NRGR, NRH2, NRHD, NRCO, NRCI, NRSI (1-based, 0 = absent) */
 int pdr_net_special_reactions(const pdr_net *net, int nr[6]);
 
+/* ---- level populations: batched FIND_CCOEFF + escape_probability + solvlevpop ----
+ * pdr_coolant_load reads a LAMDA file as read_input.F90:6-258 does (nlev and
+ * the temperature capacity ntemp as in input_parameters.F90:120-127).
+ * pdr_levpop_batched replaces, for one coolant and every cell, the calls of
+ * 3DPDR.F90:756-843: d_partner5[ncell*5] = number densities of H, H+, e-, He,
+ * H2 (find_Ccoeff.F90 argument order); d_coolant_density[ncell] = n(coolant)
+ * (the density argument of solvlevpop.F90:1); d_spop[ncell*nlev] the current
+ * populations (escape_probability's s_pop); d_tau[ncell*nlin*nrays] the
+ * line-centre optical depth of every radiative line (file order) along every
+ * ray, i.e. the ray sums of escape_probability.F90:97-106; pseudo1d uses ray 6
+ * only as PSEUDO_1D does.  Outputs: d_pop[ncell*nlev] (negatives set to 0),
+ * d_cooling[ncell] (the coolant's cooling_rate), d_line[ncell*nlev*nlev] or
+ * NULL, d_status[ncell] (1 = singular matrix) or NULL.  precision PDR_FP64
+ * solves with the reference's full-pivot Gauss-Jordan; PDR_MIXED uses an FP32
+ * Gauss-Jordan inverse plus one FP64 iterative-refinement step. */
+int pdr_coolant_load(const char *path, int nlev, int ntemp, pdr_coolant **out);
+void pdr_coolant_free(pdr_coolant *c);
+int pdr_coolant_info(const pdr_coolant *c, int *nlev, int *nlin);
+int pdr_levpop_batched(const pdr_coolant *c, int ncell, int nrays, const double *d_density,
+                       const double *d_T, const double *d_Tdust, const double *d_partner5,
+                       const double *d_coolant_density, const double *d_spop, const double *d_tau,
+                       int pseudo1d, double metallicity, double g2d, int precision, double *d_pop,
+                       double *d_cooling, double *d_line, int *d_status, void *stream);
+
+/* ---- heating: batched CALC_HEATING (sub_calculate_heating.F90:7-386) ----
+ * network 0 = reduced, 1 = full (the reference's compile-time choice of the
+ * chemical-heating reactions); d_abundance[ncell*nspec] and d_rate[ncell*nreac]
+ * in the network's species-file and rate-file order, d_uv_field[ncell] in
+ * Draine units; d_heating[ncell*12] receives HEATING_RATE(1:12) (photoelectric,
+ * PAH, Weingartner-Draine, C ionisation, H2 formation, H2 photodissociation,
+ * FUV pumping, cosmic rays, turbulence, chemical, gas-grain, total). */
+int pdr_heating_batched(const pdr_net *net, int network, const pdr_phys *phys, int ncell,
+                        const double *d_density, const double *d_Tgas, const double *d_Tdust,
+                        const double *d_uv_field, const double *d_abundance, const double *d_rate,
+                        double *d_heating, void *stream);
+
 /* ---- diagnostics (tests pin the device code against the reference with these) ----
  * The device network RHS, as the generated f() of odes_<net>.c:26-149 computes
  * it (mode 0: d_out[nstate*neq], x_e of each state in d_xe), or the analytic
