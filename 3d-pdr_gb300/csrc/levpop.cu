@@ -24,6 +24,12 @@ constexpr double KB = 1.38065040e-16, CL = 2.99792458e+10, HP = 6.62606896e-27;
 constexpr double PI = 3.141592653589793238462643383279502884197;
 constexpr unsigned FULL = 0xffffffffu;
 
+// per-warp shared memory: two nlev^2 FP64 matrices, four nlev vectors, three int vectors
+__host__ __device__ inline size_t levpop_warp_bytes(int n) {
+  auto al = [](size_t v) { return (v + 15) & ~size_t(15); };
+  return al(8 * (size_t)n * n) * 2 + al(8 * (size_t)n) * 4 + al(4 * (size_t)n) * 3;
+}
+
 struct LevArgs {
   int ncell, nrays, pseudo1d;
   double metallicity, g2d;
@@ -119,14 +125,15 @@ __global__ void __launch_bounds__(256) levpop_kernel(const __grid_constant__ Coo
   const int n = C.nlev, nn = n * n;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   auto al = [](size_t v) { return (v + 15) & ~size_t(15); };
-  const size_t per_warp = al(8 * nn) * 2 + al(8 * n) * 3 + al(4 * n) * 3;
+  const size_t per_warp = levpop_warp_bytes(n);
   unsigned char *base = smem + per_warp * warp;
   double *R = reinterpret_cast<double *>(base);              // rates, then the solvlevpop matrix
   double *aux = reinterpret_cast<double *>(base + al(8 * nn)); // line values, then FP32 matrix
   double *b = reinterpret_cast<double *>(base + 2 * al(8 * nn));
   double *sp = b + al(8 * n) / 8;
   double *x = sp + al(8 * n) / 8;
-  int *ipiv = reinterpret_cast<int *>(reinterpret_cast<unsigned char *>(x) + al(8 * n));
+  double *rs = x + al(8 * n) / 8;    // row scales of the FP32 solve
+  int *ipiv = reinterpret_cast<int *>(reinterpret_cast<unsigned char *>(rs) + al(8 * n));
   int *indxr = ipiv + al(4 * n) / 4;
   int *indxc = indxr + al(4 * n) / 4;
   const int wpb = blockDim.x >> 5;
@@ -241,24 +248,31 @@ __global__ void __launch_bounds__(256) levpop_kernel(const __grid_constant__ Coo
       ok = gauss_jordan<double>(R, b, n, ipiv, indxr, indxc, false);
       for (int i = lane; i < n; i += 32) x[i] = b[i];
     } else {
+      // rows equilibrated by their largest entry, FP32 Gauss-Jordan inverse of
+      // D M, then x = inv D b and one FP64 refinement x += inv D (b - M x)
       float *Mf = reinterpret_cast<float *>(aux);
       float *bf = Mf + nn;
-      for (int e = lane; e < nn; e += 32) Mf[e] = (float)R[e];
+      for (int i = lane; i < n; i += 32) {
+        double mx = 0.0;
+        for (int l = 0; l < n; l++) mx = fmax(mx, fabs(R[i * n + l]));
+        rs[i] = (mx > 0.0) ? 1.0 / mx : 1.0;
+      }
+      __syncwarp();
+      for (int e = lane; e < nn; e += 32) Mf[e] = (float)(R[e] * rs[e / n]);
       for (int i = lane; i < n; i += 32) bf[i] = 0.0f;
       __syncwarp();
-      ok = gauss_jordan<float>(Mf, bf, n, ipiv, indxr, indxc, true);   // Mf := approximate inverse
+      ok = gauss_jordan<float>(Mf, bf, n, ipiv, indxr, indxc, true);   // Mf := inverse of D M
       __syncwarp();
-      // x0 = inv b ; r = b - M x0 (FP64) ; x = x0 + inv r
       for (int i = lane; i < n; i += 32) {
         double s = 0.0;
-        for (int l = 0; l < n; l++) s = fma((double)Mf[i * n + l], b[l], s);
+        for (int l = 0; l < n; l++) s = fma((double)Mf[i * n + l], rs[l] * b[l], s);
         x[i] = s;
       }
       __syncwarp();
       for (int i = lane; i < n; i += 32) {
         double s = b[i];
         for (int l = 0; l < n; l++) s = fma(-R[i * n + l], x[l], s);
-        sp[i] = s;   // residual (s_pop no longer needed)
+        sp[i] = s * rs[i];   // scaled residual (s_pop is no longer needed)
       }
       __syncwarp();
       for (int i = lane; i < n; i += 32) {
@@ -280,10 +294,7 @@ __global__ void __launch_bounds__(256) levpop_kernel(const __grid_constant__ Coo
 
 }  // namespace
 
-size_t levpop_smem_per_warp(int n) {
-  auto al = [](size_t v) { return (v + 15) & ~size_t(15); };
-  return al(8 * (size_t)n * n) * 2 + al(8 * n) * 3 + al(4 * n) * 3;
-}
+size_t levpop_smem_per_warp(int n) { return levpop_warp_bytes(n); }
 
 int launch_levpop(const pdr_coolant *c, const LevArgsHost &h, bool mixed, int sm_count, cudaStream_t st) {
   LevArgs A;

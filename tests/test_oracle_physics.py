@@ -140,3 +140,46 @@ def test_levpop_conservation(key):
     assert st == 0
     assert np.allclose(pop.sum(axis=1), dens, rtol=1e-5)
     assert np.isfinite(cool).all()
+
+
+def test_levpop_conditioning():
+    """Perturbing the solvlevpop matrix of the oracle by one ulp (random
+    relative 2.2e-16 per entry) moves populations of 1e-12..1e-6 of the
+    coolant density by up to ~1e-6..1e-5 relative, while populations above
+    1e-6 of it move by < 1e-9: the bound behind the GPU level-population
+    tolerances."""
+    import ctypes as C
+    lib = O.lib()
+    lib.orc_find_ccoeff.argtypes = [C.POINTER(O.OrcCoolant), C.c_double, O._dp, O._dp]
+    lib.orc_escape_probability.argtypes = [C.POINTER(O.OrcCoolant), O._dp, O._dp, O._dp, C.c_int, C.c_int,
+                                           C.c_double, C.c_double, C.c_double, C.c_double, O._dp, O._dp, O._dp]
+    oc = O.Coolant("CO")
+    lp = W.levpop(ncell=16, seed=21)
+    tau = W.levpop_tau(16, oc.nlin, seed=22)
+    dens = lp["n_H"] * W.COOLANT_X["CO"]
+    spop = np.array([oc.lte(T, d) for T, d in zip(lp["T"], dens)])
+    n = oc.nlev
+    worst_small = worst_big = 0.0
+    for c in range(16):
+        Cm, R, L, cool = np.zeros(n * n), np.zeros(n * n), np.zeros(n * n), C.c_double()
+        lib.orc_find_ccoeff(oc.p, lp["T"][c], O._ptr(np.ascontiguousarray(lp["partner5"][c])), O._ptr(Cm))
+        lib.orc_escape_probability(oc.p, O._ptr(Cm), O._ptr(np.ascontiguousarray(spop[c])),
+                                   O._ptr(np.ascontiguousarray(tau[c])), 12, 0, lp["Td"][c], lp["n_H"][c], 1.0,
+                                   100.0, O._ptr(R), O._ptr(L), C.byref(cool))
+        R = R.reshape(n, n)
+        A = R.T.copy()
+        np.fill_diagonal(A, -R.sum(axis=1))
+        A[-1, :] = 1e-8
+        b = np.zeros(n)
+        b[-1] = dens[c] * 1e-8
+        x = np.linalg.solve(A, b)
+        rng = np.random.Generator(np.random.PCG64(c))
+        xp = np.linalg.solve(A * (1 + 2.2e-16 * rng.standard_normal(A.shape)), b)
+        rel = np.abs(xp - x) / np.maximum(np.abs(x), 1e-300)
+        small = (np.abs(x) > 1e-12 * dens[c]) & (np.abs(x) <= 1e-6 * dens[c])
+        big = np.abs(x) > 1e-6 * dens[c]
+        if small.any():
+            worst_small = max(worst_small, rel[small].max())
+        worst_big = max(worst_big, rel[big].max())
+    assert worst_big < 1e-9
+    assert worst_small > 1e-7
