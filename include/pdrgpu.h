@@ -84,6 +84,21 @@ int pdr_chem_solve_batched(const pdr_net *net, int ncell, double *d_abundance,
                            const double *d_t_end_yr, const pdr_chem_opts *opts, int *d_status,
                            int *d_stats, void *stream);
 
+/* Allocation-free variant of pdr_chem_solve_batched, with no counterpart in
+ * the reference.  For callers that cannot call cudaMalloc (device memory owned
+ * and capped by another framework's pool; serving loops that must not
+ * allocate, and so synchronise the device, once running): the solver's scratch
+ * (work-queue cursors, FP64 re-solve list) lives in a static device array of
+ * at most 262,144 cells, which every GPU that loads the library holds until
+ * exit.  Larger calls fail with PDR_E_ARG.  All calls on a device share the
+ * array: calls that overlap on the GPU race and must be serialised by the
+ * caller.  The first call on a device looks the array up with
+ * cudaGetSymbolAddress; make it before any stream capture. */
+int pdr_chem_solve_batched_noalloc(const pdr_net *net, int ncell, double *d_abundance,
+                                   const double *d_rate, const double *d_density,
+                                   const double *d_t_end_yr, const pdr_chem_opts *opts,
+                                   int *d_status, int *d_stats, void *stream);
+
 /* Legacy symbol with the reference's exact signature (calculate_abundances.c:64):
  * host arrays, all arguments by reference (gfortran implicit interface).
  * Tolerances, times and the electron index are read from the Fortran module
