@@ -1,0 +1,582 @@
+// bdf_core.cuh -- the CVODE-method BDF control logic shared by the
+// warp-per-cell (chem_warp.cu) and CTA-per-cell (chem_cta.cu) integrators.
+//
+// It restates the published SUNDIALS CVODE method step for step -- the same
+// algorithm as the CPU oracle (oracle/orc_bdf.c, which lists the sources and
+// constants): fixed-leading-coefficient BDF of order 1..5 in Nordsieck form,
+// Newton iteration with at most 3 corrections and CVODE's convergence and
+// divergence tests, the WRMS local error test, CVODE's step-size and order
+// selection, error- and convergence-failure recovery, the initial-step
+// estimate, and the tout ladder of calculate_abundances.c:214-305 with its
+// retry rules.  Every thread of the group owns one species (or none); the
+// group type D supplies the collectives and the linear algebra:
+//   bool owns; bool leader();  void sync();
+//   double sum_all(double); double max_all(double);
+//   double rhs(double y_own);  bool setup(double y_own);  double solve(double b_own);
+// Norms are kept squared (the tests compare squares, no sqrt); the step-ratio
+// heuristics eta = 1/((bias*e)^(1/k) + 1e-6) are evaluated in FP32.
+#pragma once
+
+#include "pdr_internal.h"
+
+namespace pdr {
+namespace bdf {
+
+constexpr int QMAX = 5;
+constexpr int MXNCF = 10, MXNEF = 7, MXNEF1 = 3, SMALL_NEF = 2, LONG_WAIT = 10, SMALL_NST = 10;
+constexpr int MAXCOR = 3, MSBP = 20;
+constexpr double CRDOWN = 0.3, DGMAX = 0.3, RDIV = 2.0, NLSCOEF = 0.1;
+constexpr double ETAMX1 = 10000.0, ETAMX2 = 10.0, ETAMX3 = 10.0, ETAMXF = 0.2, ETAMIN = 0.1;
+constexpr double ETACF = 0.25, ADDON = 1e-6, BIAS1 = 6.0, BIAS2 = 6.0, BIAS3 = 10.0, THRESH = 1.5;
+constexpr double YEAR = 3.1556926e7;
+constexpr int FELL_BACK = 1;   // internal status: redo this cell in FP64
+
+// shared memory of one integrator: arrays every thread reads
+struct CoefShared {
+  double tau[QMAX + 2];
+  double l[QMAX + 1];
+  double tq[6];   // tq[0] = 1/l[1], tq[1..5] error constants
+  // coefficients of a uniform step history (xi_j = j), per order 1..5
+  double ul[QMAX + 1][QMAX + 1];
+  double utq[QMAX + 1][6];
+};
+
+// squared-norm form of eta = 1/((bias*e)^(1/k) + 1e-6) with e2 = e^2 (FP32)
+__device__ __forceinline__ double eta_of(double e2, float bias, int k) {
+  const float v = powf(bias * bias * (float)e2, 0.5f / (float)k);
+  return (double)(1.0f / (v + (float)ADDON));
+}
+
+// 1/x to double precision: FP32 seed and two Newton steps
+__device__ __forceinline__ double rcp_nr(double x) {
+  double r = (double)__frcp_rn((float)x);
+  r = r * fma(-x, r, 2.0);
+  r = r * fma(-x, r, 2.0);
+  return r;
+}
+
+template <class D>
+struct Core {
+  __device__ __forceinline__ D &self() { return *static_cast<D *>(this); }
+  CoefShared *ws = nullptr;
+  // Nordsieck row of this thread's species, weight, correction, work values
+  double z[QMAX + 1];
+  double ewt, acor, y, ftmp, tmp;
+  // uniform integrator scalars
+  double tn, h, hscale, hprime, eta, etamax, saved_tq5, gamma, gammap, inv_gammap, gamrat, gscale, rl1;
+  double crate2, acnrm2;
+  double xe_last, rtol, atol;
+  int q, qprime, qwait, jcur;
+  int nst, nstlp, nfe, nje, nsetups, nni, ncfn, netf;
+  long long mxstep, max_total_steps;
+
+  __device__ __forceinline__ double wrms2(double v) {
+    const double t = self().owns ? v * ewt : 0.0;
+    return self().sum_all(t * t) * self().inv_n;
+  }
+
+  __device__ __forceinline__ void set_ewt() { ewt = self().owns ? rcp_nr(rtol * fabs(z[0]) + atol) : 0.0; }
+
+  // Pascal-triangle prediction z <- z P (and its inverse), q-specialised
+  template <int Q, int SIGN>
+  __device__ __forceinline__ void pascal() {
+#pragma unroll
+    for (int k = 1; k <= Q; k++)
+#pragma unroll
+      for (int j = Q; j >= k; j--) z[j - 1] = (SIGN > 0) ? z[j - 1] + z[j] : z[j - 1] - z[j];
+  }
+  template <int SIGN>
+  __device__ __forceinline__ void pascal_q() {
+    switch (q) {
+      case 1: pascal<1, SIGN>(); break;
+      case 2: pascal<2, SIGN>(); break;
+      case 3: pascal<3, SIGN>(); break;
+      case 4: pascal<4, SIGN>(); break;
+      default: pascal<5, SIGN>(); break;
+    }
+  }
+  __device__ __forceinline__ void predict() { tn += h; pascal_q<1>(); }
+  __device__ __forceinline__ void restore(double saved_t) { tn = saved_t; pascal_q<-1>(); }
+
+  __device__ __forceinline__ void rescale() {
+    double fac = eta;
+#pragma unroll
+    for (int j = 1; j <= QMAX; j++)
+      if (j <= q) { z[j] *= fac; fac *= eta; }
+    h = hscale * eta;
+    hscale = h;
+  }
+
+  // order q -> q-1: remove the x^q term keeping the value and slope at t_n and
+  // the values at t_{n-1}..t_{n-q+2}: z_j -= d_j z_q, d = x^2 prod_{k<=q-2}(x+xi_k)
+  __device__ __forceinline__ void decrease_order() {
+    if (q <= 2) return;
+    double d[QMAX + 2];
+#pragma unroll
+    for (int j = 0; j < QMAX + 2; j++) d[j] = 0.0;
+    d[2] = 1.0;
+    double hsum = 0.0;
+#pragma unroll
+    for (int k = 1; k <= QMAX - 2; k++) {
+      if (k <= q - 2) {
+        hsum += ws->tau[k];
+        const double xi = hsum / hscale;
+#pragma unroll
+        for (int j = QMAX + 1; j >= 1; j--) d[j] = d[j - 1] + d[j] * xi;
+        d[0] *= xi;
+      }
+    }
+    double zq = 0.0;
+#pragma unroll
+    for (int j = 0; j <= QMAX; j++) if (j == q) zq = z[j];
+#pragma unroll
+    for (int j = 2; j < QMAX; j++)
+      if (j < q) z[j] -= d[j] * zq;
+  }
+
+  // order q -> q+1: add c x^2 prod_{k<q}(x+xi_k) so the polynomial also passes
+  // through y_{n-q}; c = (sum_{j<=q} 1/j - sum_{i<=q} 1/xi_i)/prod_{i=2}^q xi_i * Delta_n
+  __device__ __forceinline__ void increase_order() {
+    double d[QMAX + 2];
+#pragma unroll
+    for (int j = 0; j < QMAX + 2; j++) d[j] = 0.0;
+    d[2] = 1.0;
+    double hsum = hscale, sum_j = 1.0, sum_xi = 1.0, prod = 1.0, xi_prev = 1.0;
+#pragma unroll
+    for (int k = 2; k <= QMAX; k++) {
+      if (k <= q) {
+        hsum += ws->tau[k];
+        const double xi = hsum / hscale;
+        sum_j += 1.0 / k;
+        sum_xi += 1.0 / xi;
+        prod *= xi;
+#pragma unroll
+        for (int j = QMAX + 1; j >= 1; j--) d[j] = d[j - 1] + d[j] * xi_prev;
+        d[0] *= xi_prev;
+        xi_prev = xi;
+      }
+    }
+    const double c = (sum_j - sum_xi) / prod;
+    const double zn1 = c * z[QMAX];
+#pragma unroll
+    for (int j = 2; j <= QMAX; j++)
+      if (j <= q) z[j] += d[j] * zn1;
+#pragma unroll
+    for (int j = 2; j <= QMAX; j++)
+      if (j == q + 1) z[j] = zn1;
+  }
+
+  // Fixed-leading-coefficient BDF coefficients l[0..q] and error constants
+  // tq[1..5] for step h and step history tau[1..q] (q+1 for tq[3])
+  __device__ __forceinline__ static void coeffs(int q, bool order_change_due, double h, const double *tau,
+                                                double *l, double *tq) {
+#pragma unroll
+    for (int j = 0; j <= QMAX; j++) l[j] = 0.0;
+    l[0] = l[1] = 1.0;
+    double a0 = -1.0, a0hat = -1.0, xi_inv = 1.0, xistar_inv = 1.0, hsum = h;
+    if (q > 1) {
+#pragma unroll
+      for (int j = 2; j < QMAX; j++) {
+        if (j < q) {
+          hsum += tau[j - 1];
+          xi_inv = h / hsum;
+          a0 -= 1.0 / j;
+#pragma unroll
+          for (int i = QMAX; i >= 1; i--)
+            if (i <= j) l[i] += l[i - 1] * xi_inv;
+        }
+      }
+      a0 -= 1.0 / q;
+      xistar_inv = -l[1] - a0;
+      hsum += tau[q - 1];
+      xi_inv = h / hsum;
+      a0hat = -l[1] - xi_inv;
+#pragma unroll
+      for (int i = QMAX; i >= 1; i--)
+        if (i <= q) l[i] += l[i - 1] * xistar_inv;
+    }
+    double lq = 0.0;
+#pragma unroll
+    for (int j = 0; j <= QMAX; j++) if (j == q) lq = l[j];
+    const double A1 = 1.0 - a0hat + a0, A2 = 1.0 + q * A1;
+    tq[2] = fabs(A1 / (a0 * A2));
+    tq[5] = fabs(A2 * xistar_inv / (lq * xi_inv));
+    if (order_change_due) {
+      if (q > 1) {
+        const double C = xistar_inv / lq, A3 = a0 + 1.0 / q, A4 = a0hat + xi_inv;
+        tq[1] = fabs(C * (1.0 - A4 + A3) / A3);
+      } else {
+        tq[1] = 1.0;
+      }
+      hsum += tau[q];
+      xi_inv = h / hsum;
+      const double A5 = a0 - 1.0 / (q + 1), A6 = a0hat - xi_inv;
+      tq[3] = fabs(((1.0 - A6 + A5) / A2) / (xi_inv * (q + 2) * A5));
+    }
+    tq[4] = NLSCOEF / tq[2];
+  }
+
+  // the table of uniform-history coefficients (h = tau_j = 1)
+  __device__ __forceinline__ void build_uniform_table() {
+    double one[QMAX + 2];
+#pragma unroll
+    for (int j = 0; j < QMAX + 2; j++) one[j] = 1.0;
+    for (int qq = 1; qq <= QMAX; qq++) {
+      double l[QMAX + 1], tq[6];
+      coeffs(qq, true, 1.0, one, l, tq);
+      self().sync();
+      if (self().leader()) {
+        for (int j = 0; j <= QMAX; j++) ws->ul[qq][j] = l[j];
+        ws->utq[qq][0] = 1.0 / l[1];
+        for (int j = 1; j <= 5; j++) ws->utq[qq][j] = tq[j];
+      }
+    }
+    self().sync();
+  }
+
+  __device__ __forceinline__ void set_coeffs() {
+    // a history of equal steps gives xi_j = j exactly: take the tabulated values
+    bool uniform = true;
+#pragma unroll
+    for (int j = 1; j <= QMAX; j++)
+      if (j <= q && ws->tau[j] != h) uniform = false;
+    self().sync();
+    if (uniform) {
+      if (self().leader()) {
+#pragma unroll
+        for (int j = 0; j <= QMAX; j++) ws->l[j] = ws->ul[q][j];
+        ws->tq[0] = ws->utq[q][0];
+        ws->tq[2] = ws->utq[q][2];
+        ws->tq[4] = ws->utq[q][4];
+        ws->tq[5] = ws->utq[q][5];
+        if (qwait == 1) { ws->tq[1] = ws->utq[q][1]; ws->tq[3] = ws->utq[q][3]; }
+      }
+    } else {
+      double l[QMAX + 1], tq[6];
+      tq[1] = ws->tq[1];
+      tq[3] = ws->tq[3];
+      coeffs(q, qwait == 1, h, ws->tau, l, tq);
+      if (self().leader()) {
+#pragma unroll
+        for (int j = 0; j <= QMAX; j++) ws->l[j] = l[j];
+        ws->tq[0] = 1.0 / l[1];
+        ws->tq[1] = tq[1]; ws->tq[2] = tq[2]; ws->tq[3] = tq[3]; ws->tq[4] = tq[4]; ws->tq[5] = tq[5];
+      }
+    }
+    self().sync();
+    rl1 = ws->tq[0];
+    gamma = h * rl1;
+    if (nst == 0) { gammap = gamma; inv_gammap = 1.0 / gamma; }
+    gamrat = (nst > 0) ? gamma * inv_gammap : 1.0;
+    gscale = (gamrat != 1.0) ? 2.0 * rcp_nr(1.0 + gamrat) : 1.0;
+  }
+
+  // called by D::setup after forming the matrix
+  __device__ __forceinline__ void after_setup() {
+    nje++;
+    nsetups++;
+    jcur = 1;
+    crate2 = 1.0;
+    gammap = gamma;
+    inv_gammap = 1.0 / gamma;
+    gamrat = 1.0;
+    gscale = 1.0;
+    nstlp = nst;
+  }
+
+  // 0 solved, 1 convergence failure, 2 failure that sends the cell to the FP64 pass
+  __device__ __forceinline__ int nls(bool prev_fail, bool fallback_on_fail) {
+    bool call_setup = prev_fail || (nst == 0) || (nst >= nstlp + MSBP) || (fabs(gamrat - 1.0) > DGMAX);
+    const double tq4 = ws->tq[4];
+    const double tq4sq = tq4 * tq4;
+    const int fail = fallback_on_fail ? 2 : 1;
+    for (int attempt = 0; attempt < 2; attempt++) {
+      y = z[0];
+      ftmp = self().rhs(y);
+      if (call_setup) {
+        if (!self().setup(y)) return fail;
+        call_setup = false;
+      }
+      acor = 0.0;
+      double delp2 = 0.0;
+      int mcor = 0;
+      bool conv = false;
+      for (;;) {
+        tmp = gamma * ftmp - (rl1 * z[1] + acor);
+        tmp = self().solve(tmp) * gscale;
+        nni++;
+        const double del2 = wrms2(tmp);
+        acor += tmp;
+        y = z[0] + acor;
+        if (mcor > 0) crate2 = fmax(CRDOWN * CRDOWN * crate2, del2 / delp2);
+        if (del2 * fmin(1.0, crate2) <= tq4sq) {
+          acnrm2 = (mcor == 0) ? del2 : wrms2(acor);
+          jcur = 0;
+          conv = true;
+          break;
+        }
+        mcor++;
+        if (mcor == MAXCOR || (mcor >= 2 && del2 > RDIV * RDIV * delp2)) break;
+        delp2 = del2;
+        ftmp = self().rhs(y);
+      }
+      if (conv) return 0;
+      if (!jcur) { call_setup = true; continue; }
+      return fail;
+    }
+    return fail;
+  }
+
+  __device__ __forceinline__ void set_eta() {
+    if (eta < THRESH) { eta = 1.0; hprime = h; }
+    else { eta = fmin(eta, etamax); hprime = h * eta; }
+  }
+
+  // one internal step: 0 ok, CVODE flag (<0), or FELL_BACK
+  __device__ __forceinline__ int step(bool fallback_on_fail) {
+    const double saved_t = tn;
+    int ncf = 0, nef = 0;
+    bool prev_fail = false;
+    double dsm2 = 0.0;
+    if (nst > 0 && hprime != h) {
+      if (qprime != q) {
+        if (qprime > q) increase_order();
+        else decrease_order();
+        q = qprime;
+        qwait = q + 1;
+      }
+      rescale();
+    }
+    for (;;) {
+      predict();
+      set_coeffs();
+      const int r = nls(prev_fail, fallback_on_fail);
+      if (r == 2) return FELL_BACK;
+      if (r != 0) {
+        ncfn++;
+        restore(saved_t);
+        ncf++;
+        etamax = 1.0;
+        if (ncf == MXNCF) return PDR_CONV_FAILURE;
+        eta = ETACF;
+        prev_fail = true;
+        rescale();
+        continue;
+      }
+      const double tq2 = ws->tq[2];
+      dsm2 = acnrm2 * (tq2 * tq2);
+      if (dsm2 <= 1.0) break;
+      nef++;
+      netf++;
+      prev_fail = true;
+      restore(saved_t);
+      if (nef == MXNEF) return PDR_ERR_FAILURE;
+      etamax = 1.0;
+      const int L = q + 1;
+      if (nef <= MXNEF1) {
+        eta = eta_of(dsm2, (float)BIAS2, L);
+        eta = fmax(ETAMIN, eta);
+        if (nef >= SMALL_NEF) eta = fmin(eta, ETAMXF);
+        rescale();
+        continue;
+      }
+      if (q > 1) {
+        eta = ETAMIN;
+        decrease_order();
+        q--;
+        qwait = q + 1;
+        rescale();
+        continue;
+      }
+      eta = ETAMIN;
+      h *= eta;
+      hscale = h;
+      qwait = LONG_WAIT;
+      tmp = self().rhs(z[0]);
+      z[1] = h * tmp;
+    }
+    // complete the step
+    nst++;
+    self().sync();
+    if (self().leader()) {
+#pragma unroll
+      for (int i = QMAX; i >= 2; i--)
+        if (i <= q) ws->tau[i] = ws->tau[i - 1];
+      if (q == 1 && nst > 1) ws->tau[2] = ws->tau[1];
+      ws->tau[1] = h;
+    }
+    self().sync();
+    switch (q) {
+#define PDR_CORRECT(Q) case Q: _Pragma("unroll") for (int j = 0; j <= Q; j++) z[j] = fma(ws->l[j], acor, z[j]); break;
+      PDR_CORRECT(1) PDR_CORRECT(2) PDR_CORRECT(3) PDR_CORRECT(4) PDR_CORRECT(5)
+#undef PDR_CORRECT
+    }
+    qwait--;
+    if (qwait == 1 && q != QMAX) {
+      z[QMAX] = acor;
+      saved_tq5 = ws->tq[5];
+    }
+    if (etamax == 1.0) {
+      if (qwait < 2) qwait = 2;
+      qprime = q;
+      hprime = h;
+      eta = 1.0;
+    } else {
+      const int L = q + 1;
+      const double etaq = eta_of(dsm2, (float)BIAS2, L);
+      if (qwait != 0) {
+        eta = etaq;
+        qprime = q;
+        set_eta();
+      } else {
+        qwait = 2;
+        double etaqm1 = 0.0, etaqp1 = 0.0;
+        if (q > 1) {
+          double zq = 0.0;
+#pragma unroll
+          for (int j = 0; j <= QMAX; j++) if (j == q) zq = z[j];
+          const double tq1 = ws->tq[1];
+          etaqm1 = eta_of(wrms2(zq) * (tq1 * tq1), (float)BIAS1, q);
+        }
+        if (q != QMAX && saved_tq5 != 0.0) {
+          // step-ratio factor of the order-raise estimate (heuristic, FP32)
+          const float ratio = (float)h / (float)ws->tau[2];
+          float rp = ratio;
+          for (int k = 1; k < L; k++) rp *= ratio;
+          const double cquot = (double)(((float)ws->tq[5] / (float)saved_tq5) * rp);
+          const double tq3 = ws->tq[3];
+          etaqp1 = eta_of(wrms2(acor - cquot * z[QMAX]) * (tq3 * tq3), (float)BIAS3, L + 1);
+        }
+        // ties keep the current order, then prefer the lower one
+        const double etam = fmax(etaqm1, fmax(etaq, etaqp1));
+        if (etam < THRESH) { eta = 1.0; qprime = q; }
+        else if (etam == etaq) { eta = etaq; qprime = q; }
+        else if (etam == etaqm1) { eta = etaqm1; qprime = q - 1; }
+        else { eta = etaqp1; qprime = q + 1; z[QMAX] = acor; }
+        set_eta();
+      }
+    }
+    etamax = (nst <= SMALL_NST) ? ETAMX2 : ETAMX3;
+    return 0;
+  }
+
+  // initial step from an estimate of ||y''|| (h^2/2 ||y''|| = 1, safety 0.5)
+  __device__ __forceinline__ double initial_step(double t0, double tout) {
+    const double tdist = fabs(tout - t0);
+    const double tround = 2.220446049250313e-16 * fmax(fabs(t0), fabs(tout));
+    const double hlb = 100.0 * tround;
+    const double hub_inv = self().max_all(self().owns ? fabs(z[1]) / (0.1 * fabs(z[0]) + atol) : 0.0);
+    double hub = 0.1 * tdist;
+    if (hub * hub_inv > 1.0) hub = 1.0 / hub_inv;
+    double hg = sqrt(hlb * hub);
+    if (hub < hlb) return hg;
+    bool ok = false;
+    double hnew = hg;
+    for (int it = 1; it <= 4; it++) {
+      tmp = self().rhs(z[0] + hg * z[1]);
+      const double yddnrm = sqrt(wrms2((tmp - z[1]) / hg));
+      if (ok || it == 4) { hnew = hg; break; }
+      hnew = (yddnrm * hub * hub > 2.0) ? sqrt(2.0 / yddnrm) : sqrt(hg * hub);
+      const double hrat = hnew / hg;
+      if (hrat > 0.5 && hrat < 2.0) ok = true;
+      if (it > 1 && hrat > 2.0) { hnew = hg; ok = true; }
+      hg = hnew;
+    }
+    double h0 = 0.5 * hnew;
+    if (h0 < hlb) h0 = hlb;
+    if (h0 > hub) h0 = hub;
+    return h0;
+  }
+
+  __device__ __forceinline__ double interpolate(double t) const {
+    const double s = (t - tn) / hscale;
+    double v = 0.0;
+#pragma unroll
+    for (int j = QMAX; j >= 0; j--)
+      if (j <= q) v = (j == q) ? z[j] : fma(s, v, z[j]);
+    return v;
+  }
+
+  // CVode(..., CV_NORMAL) from the current state to tout
+  __device__ __forceinline__ int solve_to(double tout, bool first, double t0, long long &total, bool fb) {
+    if (first) {
+      set_ewt();
+      z[1] = self().rhs(z[0]);
+      const double h0 = initial_step(t0, tout);
+      z[1] *= h0;
+      h = hscale = hprime = h0;
+      q = qprime = 1;
+      qwait = 2;
+      etamax = ETAMX1;
+      nst = 0;
+    } else if ((tn - tout) * h >= 0.0) {
+      return 0;
+    }
+    long long nstloc = 0;
+    for (;;) {
+      if (nst > 0) set_ewt();
+      if (nstloc >= mxstep || total >= max_total_steps) return PDR_TOO_MUCH_WORK;
+      const int kf = step(fb);
+      if (kf != 0) return kf;
+      nstloc++;
+      total++;
+      if ((tn - tout) * h >= 0.0) return 0;
+    }
+  }
+
+  // calculate_abundances.c:132-317 for one cell from z[0] = y0: returns the
+  // cell's status (CVODE flag, or FELL_BACK) and the output value of this
+  // thread's species in *yout (interpolated at the last tout, or z[0] after a
+  // failing call), before the abstol clamp
+  __device__ __forceinline__ int integrate(double t0_yr, double tend_yr, bool fb, double *yout) {
+    if (self().leader()) {
+#pragma unroll
+      for (int j = 0; j < QMAX + 2; j++) ws->tau[j] = 0.0;
+#pragma unroll
+      for (int j = 0; j < 6; j++) ws->tq[j] = 0.0;
+    }
+    self().sync();
+    nfe = nje = nsetups = nni = ncfn = netf = 0;
+    nst = nstlp = 0;
+    saved_tq5 = 0.0;
+    crate2 = 1.0;
+    gammap = gamma = 1.0;
+    inv_gammap = 1.0;
+    gamrat = 1.0;
+    gscale = 1.0;
+    jcur = 0;
+    acor = 0.0;
+    const double t0 = t0_yr * YEAR, tend = tend_yr * YEAR;
+    tn = t0;
+    double tout = 1.0e-4 * YEAR, t = t0;
+    int nfails = 0, status = 0, lastflag = 0;
+    long long total = 0;
+    bool first = true;
+    double tlast = tout;
+    do {
+      const int flag = solve_to(tout, first, t0, total, fb);
+      first = false;
+      if (flag == FELL_BACK) return FELL_BACK;
+      lastflag = flag;
+      tlast = tout;
+      if (flag != 0) {
+        nfails++;
+        if (!((flag == PDR_TOO_MUCH_WORK || flag == PDR_CONV_FAILURE) && nfails < 5)) {
+          status = flag;
+          if (flag != PDR_TOO_MUCH_WORK && flag != PDR_CONV_FAILURE) nfails = 5;
+        }
+        if (total >= max_total_steps) { status = PDR_TOO_MUCH_WORK; nfails = 5; }
+        t = tn;
+      } else {
+        t = tout;
+      }
+      tout = tout * 10.0;
+      if (tout > tend) tout = tend;
+    } while (t < tout && nfails < 5);
+    *yout = (lastflag == 0) ? interpolate(tlast) : z[0];
+    return status;
+  }
+};
+
+}  // namespace bdf
+}  // namespace pdr

@@ -113,6 +113,8 @@ void pdr_chem_opts_default(pdr_chem_opts *o) {
   o->precision = PDR_FP64;
   o->warps_per_block = 0;
   o->blocks_per_sm = 0;
+  o->reg_variant = 0;
+  o->refill = 0;
 }
 
 int pdr_device_info(int *sm_count, int *cc_major, int *cc_minor) {
@@ -212,6 +214,54 @@ int pdr_chem_solve_batched(const pdr_net *net, int ncell, double *d_abundance, c
     if (rc) return rc;
   }
   return 0;
+}
+
+int pdr_chem_autotune(const pdr_net *net, int ncell_sample, const double *d_abundance, const double *d_rate,
+                      const double *d_density, pdr_chem_opts *opts, void *stream) {
+  if (!net || ncell_sample <= 0 || !d_abundance || !d_rate || !d_density || !opts) {
+    set_error("pdr_chem_autotune: invalid argument");
+    return PDR_E_ARG;
+  }
+  const int ns = net->host.nspec;
+  cudaStream_t st = (cudaStream_t)stream;
+  double *ab = nullptr;
+  int *status = nullptr;
+  cudaError_t e = cudaMalloc(&ab, sizeof(double) * (size_t)ncell_sample * ns);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(autotune)");
+  e = cudaMalloc(&status, sizeof(int) * (size_t)ncell_sample);
+  if (e != cudaSuccess) { cudaFree(ab); return cuda_fail(e, "cudaMalloc(autotune)"); }
+  cudaEvent_t t0, t1;
+  cudaEventCreate(&t0);
+  cudaEventCreate(&t1);
+  struct Cand { int wpb, reg, refill; };
+  const Cand cands[] = {{4, 0, 0}, {2, 0, 0}, {8, 0, 0}, {4, 1, 0}, {8, 1, 0}, {4, 0, 1}};
+  float best = 1e30f;
+  pdr_chem_opts best_o = *opts;
+  int rc = 0;
+  for (const Cand &c : cands) {
+    pdr_chem_opts o = *opts;
+    o.warps_per_block = c.wpb;
+    o.reg_variant = c.reg;
+    o.refill = c.refill;
+    o.blocks_per_sm = 0;
+    e = cudaMemcpyAsync(ab, d_abundance, sizeof(double) * (size_t)ncell_sample * ns, cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) { rc = cuda_fail(e, "autotune copy"); break; }
+    cudaEventRecord(t0, st);
+    rc = pdr_chem_solve_batched(net, ncell_sample, ab, d_rate, d_density, nullptr, &o, status, nullptr, st);
+    if (rc) break;
+    cudaEventRecord(t1, st);
+    e = cudaEventSynchronize(t1);
+    if (e != cudaSuccess) { rc = cuda_fail(e, "autotune run"); break; }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, t0, t1);
+    if (ms < best) { best = ms; best_o = o; }
+  }
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  cudaFree(ab);
+  cudaFree(status);
+  if (rc == 0) *opts = best_o;
+  return rc;
 }
 
 int pdr_rates_batched(const pdr_net *net, const pdr_phys *phys, int ncell, int nrays, const double *d_T,

@@ -13,8 +13,10 @@
 //   1e-8, rhs = density*1e-8, solvlevpop.F90:18-35) held in shared memory and
 //   solved either in FP64 by the reference's Gauss-Jordan elimination with full
 //   pivoting (same pivot order, unfused products as in the reference), or by
-//   FP32 Gauss-Jordan giving an approximate inverse plus one FP64
-//   iterative-refinement step; negative populations are set to zero.
+//   a row-equilibrated FP32 Gauss-Jordan inverse plus one FP64
+//   iterative-refinement step, verified by the size of the next correction
+//   (cells that fail the check are re-solved in FP64, status 2); negative
+//   populations are set to zero.
 #include "pdr_internal.h"
 
 namespace pdr {
@@ -243,7 +245,7 @@ __global__ void __launch_bounds__(256) levpop_kernel(const __grid_constant__ Coo
     const double dens = A.cdens[cell];
     if (lane == 0) b[n - 1] = dens * 1.0e-8;
     __syncwarp();
-    bool ok;
+    bool ok, redo = false;
     if constexpr (!MIXED) {
       ok = gauss_jordan<double>(R, b, n, ipiv, indxr, indxc, false);
       for (int i = lane; i < n; i += 32) x[i] = b[i];
@@ -279,6 +281,38 @@ __global__ void __launch_bounds__(256) levpop_kernel(const __grid_constant__ Coo
         double s = 0.0;
         for (int l = 0; l < n; l++) s = fma((double)Mf[i * n + l], sp[l], s);
         x[i] += s;
+        bf[i] = (float)fabs(s);   // size of the first correction
+      }
+      __syncwarp();
+      // verify with the correction a second refinement would make: for every
+      // population above 1e-14 of the coolant density it must be below 1e-8
+      // of the population and at most half of the first correction (the
+      // refinement contracts, so the remaining error is bounded by it);
+      // otherwise the cell is re-solved by the FP64 Gauss-Jordan (R is intact)
+      for (int i = lane; i < n; i += 32) {
+        double s = b[i];
+        for (int l = 0; l < n; l++) s = fma(-R[i * n + l], x[l], s);
+        sp[i] = s * rs[i];
+      }
+      __syncwarp();
+      bool bad = false;
+      for (int i = lane; i < n; i += 32) {
+        double s = 0.0;
+        for (int l = 0; l < n; l++) s = fma((double)Mf[i * n + l], sp[l], s);
+        const double ax = fabs(x[i]), as = fabs(s);
+        const bool small = as <= 1.0e-8 * ax;
+        const bool contracts = as <= 0.5 * (double)bf[i] || as <= 1.0e-12 * ax;
+        if (ax > 1.0e-14 * dens && !(small && contracts)) bad = true;
+      }
+      if (!ok || __any_sync(FULL, bad)) {
+        __syncwarp();
+        for (int i = lane; i < n; i += 32) b[i] = 0.0;
+        __syncwarp();
+        if (lane == 0) b[n - 1] = dens * 1.0e-8;
+        __syncwarp();
+        ok = gauss_jordan<double>(R, b, n, ipiv, indxr, indxc, false);
+        for (int i = lane; i < n; i += 32) x[i] = b[i];
+        redo = true;
       }
     }
     __syncwarp();
@@ -287,7 +321,7 @@ __global__ void __launch_bounds__(256) levpop_kernel(const __grid_constant__ Coo
       if (v < 0.0) v = 0.0;
       A.pop[(size_t)cell * n + i] = v;
     }
-    if (lane == 0 && A.status) A.status[cell] = ok ? 0 : 1;
+    if (lane == 0 && A.status) A.status[cell] = ok ? (redo ? 2 : 0) : 1;
     __syncwarp();
   }
 }

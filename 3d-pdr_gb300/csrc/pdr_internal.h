@@ -34,11 +34,10 @@ struct WarpTables {
   int jac_len = 0;     // Jacobian terms per species (padded)
   int2 *rab = nullptr;        // [nreac] reactant slots (a, b)
   double *nh_mask = nullptr;  // [nreac] 1 if the rate constant is multiplied by n_H
-  int *rhs_r = nullptr;       // [rhs_len][32] reaction of each term
+  int *rhs_rf = nullptr;      // [rhs_len][32] reaction | (partial slot written after the term + 1) << 16
   double *rhs_nu = nullptr;   // [rhs_len][32] stoichiometric coefficient (0 = padding)
-  int *rhs_flush = nullptr;   // [rhs_len][32] partial slot written after the term, -1 none
   int *plist = nullptr;       // [plist_len][32] partial slots of species `lane`
-  int *jac_r = nullptr;       // [jac_len][32]
+  int *jac_rab = nullptr;     // [jac_len][32] reaction | slot a << 16 | slot b << 24
   double *jac_nu = nullptr;   // [jac_len][32]
   float *jac_nu_f = nullptr;  // [jac_len][32]
   double *xe_coef = nullptr;  // [32] electron-sum coefficient per slot

@@ -240,6 +240,7 @@ int build_device_tables(pdr_net *net) {
     w.nreac = h.nreac;
     const int T = (int)terms.size();
     w.rhs_len = std::max(1, (T + kWarp - 1) / kWarp);
+    if (h.nreac >= 65536 || neq + 2 > 255) return PDR_E_NET;
     std::vector<int> rr(w.rhs_len * kWarp, 0), fl(w.rhs_len * kWarp, -1);
     std::vector<double> nu(w.rhs_len * kWarp, 0.0);
     std::vector<std::vector<int>> parts(kWarp);
@@ -268,12 +269,13 @@ int build_device_tables(pdr_net *net) {
     for (auto &t : terms) per[t.i].push_back(t);
     w.jac_len = 1;
     for (auto &p : per) w.jac_len = std::max<int>(w.jac_len, (int)p.size());
-    std::vector<int> jr(w.jac_len * kWarp, 0);
+    std::vector<int> jr(w.jac_len * kWarp, 0);   // reaction | a << 16 | b << 24
     std::vector<double> jn(w.jac_len * kWarp, 0.0);
     std::vector<float> jnf(w.jac_len * kWarp, 0.0f);
     for (int i = 0; i < kWarp; i++)
       for (size_t k = 0; k < per[i].size(); k++) {
-        jr[k * kWarp + i] = per[i][k].r;
+        const int r = per[i][k].r;
+        jr[k * kWarp + i] = r | (rab[r].x << 16) | (rab[r].y << 24);
         jn[k * kWarp + i] = per[i][k].nu;
         jnf[k * kWarp + i] = (float)per[i][k].nu;
       }
@@ -281,11 +283,12 @@ int build_device_tables(pdr_net *net) {
     for (int i = 0; i < neq; i++) xe[i] = h.xe[i];
     w.rab = upload(net, rab, rc);
     w.nh_mask = upload(net, nhm, rc);
-    w.rhs_r = upload(net, rr, rc);
+    std::vector<int> rf(rr.size());
+    for (size_t k = 0; k < rr.size(); k++) rf[k] = rr[k] | ((fl[k] + 1) << 16);
+    w.rhs_rf = upload(net, rf, rc);
     w.rhs_nu = upload(net, nu, rc);
-    w.rhs_flush = upload(net, fl, rc);
     w.plist = upload(net, pl, rc);
-    w.jac_r = upload(net, jr, rc);
+    w.jac_rab = upload(net, jr, rc);
     w.jac_nu = upload(net, jn, rc);
     w.jac_nu_f = upload(net, jnf, rc);
     w.xe_coef = upload(net, xe, rc);

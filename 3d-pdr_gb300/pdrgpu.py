@@ -24,7 +24,8 @@ _vp = C.c_void_p
 class ChemOpts(C.Structure):
     _fields_ = [("reltol", C.c_double), ("abstol", C.c_double), ("start_time_yr", C.c_double),
                 ("end_time_yr", C.c_double), ("mxstep", C.c_long), ("precision", C.c_int),
-                ("warps_per_block", C.c_int), ("blocks_per_sm", C.c_int)]
+                ("warps_per_block", C.c_int), ("blocks_per_sm", C.c_int), ("reg_variant", C.c_int),
+                ("refill", C.c_int)]
 
 
 class Phys(C.Structure):
@@ -68,6 +69,7 @@ def lib():
     L.pdr_calculate_abundances.argtypes = [_vp, _vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_int,
                                            C.POINTER(ChemOpts)]
     L.pdr_probe_fma_tflops.argtypes = [C.c_int, C.POINTER(C.c_double), _vp]
+    L.pdr_chem_autotune.argtypes = [_vp, C.c_int, _vp, _vp, _vp, C.POINTER(ChemOpts), _vp]
     L.pdr_heating_batched.argtypes = [_vp, C.c_int, C.POINTER(Phys), C.c_int] + [_vp] * 8
     L.pdr_coolant_load.argtypes = [C.c_char_p, C.c_int, C.c_int, C.POINTER(_vp)]
     L.pdr_coolant_free.argtypes = [_vp]
@@ -282,3 +284,11 @@ def heating(net, network, ph, density, Tgas, Tdust, uv_field, abundance, rate, s
                                     _ptr(Tgas), _ptr(Tdust), _ptr(uv_field), _ptr(abundance), _ptr(rate),
                                     _ptr(out), _stream(stream)), "pdr_heating_batched")
     return out
+
+
+def autotune(net, abundance, rate, density, opts, ncell_sample=None, stream=None):
+    """Pick the fastest launch shape on a sample of the inputs (opts updated in place)."""
+    n = abundance.shape[0] if ncell_sample is None else min(ncell_sample, abundance.shape[0])
+    check(lib().pdr_chem_autotune(net.handle, n, _ptr(abundance), _ptr(rate), _ptr(density), C.byref(opts),
+                                  _stream(stream)), "pdr_chem_autotune")
+    return opts

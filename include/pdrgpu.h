@@ -54,8 +54,10 @@ typedef struct {
   double end_time_yr;   /* end_time (params.dat), used when d_t_end_yr is NULL       */
   long mxstep;          /* max internal steps per output interval (1e7, calculate_abundances.c:111) */
   int precision;        /* PDR_FP64 or PDR_MIXED                                      */
-  int warps_per_block;  /* launch shape (0: autotuned/default)                        */
+  int warps_per_block;  /* warps (cells in flight) per block, 1..8; 0: default 4      */
   int blocks_per_sm;    /* 0: as many as fit                                          */
+  int reg_variant;      /* 0: up to ~160 registers/thread, 1: 128 (more warps per SM) */
+  int refill;           /* 0: warps refill from an atomic work queue, 1: static split */
 } pdr_chem_opts;
 
 void pdr_chem_opts_default(pdr_chem_opts *opts);
@@ -99,6 +101,14 @@ int pdr_chem_solve_batched_noalloc(const pdr_net *net, int ncell, double *d_abun
                                    const double *d_t_end_yr, const pdr_chem_opts *opts,
                                    int *d_status, int *d_stats, void *stream);
 
+/* Autotuner: times launch shapes (warps per block, register variant, refill
+ * policy) on copies of the first ncell_sample cells of the given inputs (the
+ * inputs are not modified) and writes the fastest into opts, keeping its other
+ * fields.  Allocates temporary device buffers; call it before stream capture. */
+int pdr_chem_autotune(const pdr_net *net, int ncell_sample, const double *d_abundance,
+                      const double *d_rate, const double *d_density, pdr_chem_opts *opts,
+                      void *stream);
+
 /* Legacy symbol with the reference's exact signature (calculate_abundances.c:64):
  * host arrays, all arguments by reference (gfortran implicit interface).
  * Tolerances, times and the electron index are read from the Fortran module
@@ -141,9 +151,12 @@ int pdr_net_special_reactions(const pdr_net *net, int nr[6]);
  * ray, i.e. the ray sums of escape_probability.F90:97-106; pseudo1d uses ray 6
  * only as PSEUDO_1D does.  Outputs: d_pop[ncell*nlev] (negatives set to 0),
  * d_cooling[ncell] (the coolant's cooling_rate), d_line[ncell*nlev*nlev] or
- * NULL, d_status[ncell] (1 = singular matrix) or NULL.  precision PDR_FP64
- * solves with the reference's full-pivot Gauss-Jordan; PDR_MIXED uses an FP32
- * Gauss-Jordan inverse plus one FP64 iterative-refinement step. */
+ * NULL, d_status[ncell] (0 ok, 1 singular matrix, 2 mixed solve re-done in
+ * FP64) or NULL.  precision PDR_FP64 solves with the reference's full-pivot
+ * Gauss-Jordan; PDR_MIXED uses a row-equilibrated FP32 Gauss-Jordan inverse
+ * plus one FP64 iterative-refinement step, and re-solves in FP64 the cells
+ * whose next correction would exceed 1e-7 of a population above 1e-12 of the
+ * coolant density. */
 int pdr_coolant_load(const char *path, int nlev, int ntemp, pdr_coolant **out);
 void pdr_coolant_free(pdr_coolant *c);
 int pdr_coolant_info(const pdr_coolant *c, int *nlev, int *nlin);

@@ -50,8 +50,8 @@ def test_levpop_matches_oracle(cuda, key, precision, pseudo1d):
                                                   dev(lp["Td"], cuda), dev(lp["partner5"], cuda),
                                                   dev(dens, cuda), dev(spop, cuda), dev(tau, cuda),
                                                   pseudo1d=pseudo1d, precision=precision, want_line=True)
-    pop, cool, line = pop.cpu().numpy(), cool.cpu().numpy(), line.cpu().numpy()
-    assert (status.cpu().numpy() == 0).all()
+    pop, cool, line, status = pop.cpu().numpy(), cool.cpu().numpy(), line.cpu().numpy(), status.cpu().numpy()
+    assert ((status == 0) | ((status == 2) & (precision == "mixed"))).all()
     m = pop_r > 1e-6 * dens[:, None]
     assert (np.abs(pop - pop_r)[m] / pop_r[m]).max() < TOL
     m = pop_r > 1e-12 * dens[:, None]
