@@ -17,6 +17,8 @@
 // heuristics eta = 1/((bias*e)^(1/k) + 1e-6) are evaluated in FP32.
 #pragma once
 
+#include <type_traits>
+
 #include "pdr_internal.h"
 
 namespace pdr {
@@ -55,12 +57,46 @@ __device__ __forceinline__ double rcp_nr(double x) {
   return r;
 }
 
-template <class D>
+// Nordsieck row of one thread's species held in six registers behind an
+// index operator: a constant index selects a register, a run-time index a
+// select chain -- never an address, so the integrator object is not forced
+// into local memory by an indexed array member.
+struct ZRow {
+  double v0, v1, v2, v3, v4, v5;
+  __device__ __forceinline__ double get(int j) const {
+    return j == 0 ? v0 : j == 1 ? v1 : j == 2 ? v2 : j == 3 ? v3 : j == 4 ? v4 : v5;
+  }
+  __device__ __forceinline__ void set(int j, double x) {
+    if (j == 0) v0 = x; else if (j == 1) v1 = x; else if (j == 2) v2 = x;
+    else if (j == 3) v3 = x; else if (j == 4) v4 = x; else v5 = x;
+  }
+  struct Ref {
+    ZRow &r;
+    int j;
+    __device__ __forceinline__ operator double() const { return r.get(j); }
+    __device__ __forceinline__ Ref &operator=(double x) { r.set(j, x); return *this; }
+    __device__ __forceinline__ Ref &operator=(const Ref &o) { r.set(j, (double)o); return *this; }
+    __device__ __forceinline__ Ref &operator+=(double x) { r.set(j, r.get(j) + x); return *this; }
+    __device__ __forceinline__ Ref &operator-=(double x) { r.set(j, r.get(j) - x); return *this; }
+    __device__ __forceinline__ Ref &operator*=(double x) { r.set(j, r.get(j) * x); return *this; }
+  };
+  __device__ __forceinline__ Ref operator[](int j) { return Ref{*this, j}; }
+  __device__ __forceinline__ double operator[](int j) const { return get(j); }
+};
+
+// Nordsieck row in shared memory, z[j] at p[j * s] (frees 12 registers)
+struct ZShared {
+  double *p;
+  int s;
+  __device__ __forceinline__ double &operator[](int j) const { return p[j * s]; }
+};
+
+template <class D, bool ZSHARED = false>
 struct Core {
   __device__ __forceinline__ D &self() { return *static_cast<D *>(this); }
   CoefShared *ws = nullptr;
   // Nordsieck row of this thread's species, weight, correction, work values
-  double z[QMAX + 1];
+  typename std::conditional<ZSHARED, ZShared, ZRow>::type z;
   double ewt, acor, y, ftmp, tmp;
   // uniform integrator scalars
   double tn, h, hscale, hprime, eta, etamax, saved_tq5, gamma, gammap, inv_gammap, gamrat, gscale, rl1;
@@ -83,7 +119,8 @@ struct Core {
 #pragma unroll
     for (int k = 1; k <= Q; k++)
 #pragma unroll
-      for (int j = Q; j >= k; j--) z[j - 1] = (SIGN > 0) ? z[j - 1] + z[j] : z[j - 1] - z[j];
+      for (int j = Q; j >= 1; j--)
+        if (j >= k) z[j - 1] = (SIGN > 0) ? z[j - 1] + z[j] : z[j - 1] - z[j];
   }
   template <int SIGN>
   __device__ __forceinline__ void pascal_q() {

@@ -4,6 +4,7 @@
 // semantics (calculate_abundances.c:64-354); the batched entry points take
 // device arrays and a stream so a caller can keep state resident in HBM and
 // capture the calls in a CUDA graph.
+#include <algorithm>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -26,11 +27,17 @@ extern int global_module_mp_nelect_ __attribute__((weak));
 
 namespace pdr {
 
-size_t chem_warp_smem_per_warp(int nsp, int nreac, int nparts, bool mixed);
+size_t chem_warp_smem_per_warp(int nsp, int nreac, int nparts, bool mixed, bool zshared);
 int launch_chem_warp(const pdr_net *net, int ncell, double *ab, const double *rate, const double *dens,
                      const double *tend, const pdr_chem_opts &o, int *status, int *stats, int *queue,
                      int *fb_list, int *fb_count, const int *cell_list, const int *total_ptr, bool mixed,
                      int sm_count, cudaStream_t st);
+int launch_chem_cta(const pdr_net *net, int ncell, double *ab, const double *rate, const double *dens,
+                    const double *tend, const pdr_chem_opts &o, int *status, int *stats, int *queue,
+                    int *fb_list, int *fb_count, const int *cell_list, const int *total_ptr, bool mixed,
+                    int grid, void *scratch, cudaStream_t st);
+size_t chem_cta_global_bytes(const pdr_net *net, bool mixed, int grid);
+int chem_cta_blocks_per_sm(const pdr_net *net, bool mixed);
 int launch_rates(const pdr_net *net, const pdr_phys &ph, int ncell, int nrays, const double *T,
                  const double *Td, const double *rad, const double *AV, const double *col5, double *rate,
                  int *status, int sm_count, cudaStream_t st);
@@ -72,6 +79,8 @@ struct Scratch {
   int *counters = nullptr;   // [0] queue, [1] redo queue, [2] redo count
   int *redo = nullptr;
   size_t redo_cap = 0;
+  void *cta = nullptr;       // block integrator: per-block rate constants (and matrices)
+  size_t cta_bytes = 0;
 };
 static std::mutex g_mu;
 static Scratch g_scratch[64];
@@ -95,6 +104,30 @@ static int scratch_for(int dev, size_t ncell, Scratch **out) {
   return 0;
 }
 
+static int cta_scratch(Scratch *s, size_t bytes) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (s->cta_bytes >= bytes) return 0;
+  if (s->cta) cudaFree(s->cta);
+  s->cta = nullptr;
+  s->cta_bytes = 0;
+  cudaError_t e = cudaMalloc(&s->cta, bytes);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(block integrator scratch)");
+  s->cta_bytes = bytes;
+  return 0;
+}
+
+// blocks per SM of the block integrator, cached per network and precision
+static int cta_per_sm(const pdr_net *net, bool mixed) {
+  static std::mutex mu;
+  static std::vector<std::pair<const pdr_net *, int>> cache[2];
+  std::lock_guard<std::mutex> lk(mu);
+  for (auto &c : cache[mixed])
+    if (c.first == net) return c.second;
+  const int v = chem_cta_blocks_per_sm(net, mixed);
+  if (v > 0) cache[mixed].push_back({net, v});
+  return v;
+}
+
 }  // namespace pdr
 
 using namespace pdr;
@@ -115,6 +148,7 @@ void pdr_chem_opts_default(pdr_chem_opts *o) {
   o->blocks_per_sm = 0;
   o->reg_variant = 0;
   o->refill = 0;
+  o->integrator = 0;
 }
 
 int pdr_device_info(int *sm_count, int *cc_major, int *cc_minor) {
@@ -190,8 +224,15 @@ int pdr_chem_solve_batched(const pdr_net *net, int ncell, double *d_abundance, c
     set_error("pdr_chem_solve_batched: invalid options");
     return PDR_E_ARG;
   }
-  if (!net->warp_ok || net->host.neq != 32) {
-    set_error("pdr_chem_solve_batched: this build integrates networks with 32 ODE species");
+  if (o.integrator < 0 || o.integrator > 2) {
+    set_error("pdr_chem_solve_batched: invalid integrator choice");
+    return PDR_E_ARG;
+  }
+  const bool warp_ok = net->warp_ok && net->host.neq == 32;
+  const bool warp_path = (o.integrator == 1) || (o.integrator == 0 && warp_ok);
+  if ((warp_path && !warp_ok) || (!warp_path && !net->cta_ok)) {
+    set_error(warp_path ? "pdr_chem_solve_batched: the warp integrator takes networks of 32 ODE species"
+                        : "pdr_chem_solve_batched: the network is too large for the integrator tables");
     return PDR_E_NET;
   }
   int dev = 0, sms = 0;
@@ -204,13 +245,36 @@ int pdr_chem_solve_batched(const pdr_net *net, int ncell, double *d_abundance, c
   cudaError_t e = cudaMemsetAsync(s->counters, 0, 4 * sizeof(int), st);
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(scratch)");
   const bool mixed = (o.precision == PDR_MIXED);
-  rc = launch_chem_warp(net, ncell, d_abundance, d_rate, d_density, d_t_end_yr, o, d_status, d_stats,
-                        s->counters + 0, s->redo, s->counters + 2, nullptr, nullptr, mixed, sms, st);
+  if (warp_path) {
+    rc = launch_chem_warp(net, ncell, d_abundance, d_rate, d_density, d_t_end_yr, o, d_status, d_stats,
+                          s->counters + 0, s->redo, s->counters + 2, nullptr, nullptr, mixed, sms, st);
+    if (rc) return rc;
+    if (mixed) {
+      // cells whose FP32 Newton iteration failed are re-solved in FP64
+      rc = launch_chem_warp(net, ncell, d_abundance, d_rate, d_density, d_t_end_yr, o, d_status, d_stats,
+                            s->counters + 1, nullptr, nullptr, s->redo, s->counters + 2, false, sms, st);
+      if (rc) return rc;
+    }
+    return 0;
+  }
+  // one block per cell: persistent grid of SMs x resident blocks
+  auto grid_of = [&](bool m) {
+    int per_sm = cta_per_sm(net, m);
+    if (per_sm < 1) per_sm = 1;
+    if (o.blocks_per_sm > 0 && o.blocks_per_sm < per_sm) per_sm = o.blocks_per_sm;
+    return sms * per_sm;
+  };
+  const int grid1 = grid_of(mixed), grid2 = mixed ? grid_of(false) : 0;
+  size_t bytes = chem_cta_global_bytes(net, mixed, grid1);
+  if (mixed) bytes = std::max(bytes, chem_cta_global_bytes(net, false, grid2));
+  rc = cta_scratch(s, bytes);
+  if (rc) return rc;
+  rc = launch_chem_cta(net, ncell, d_abundance, d_rate, d_density, d_t_end_yr, o, d_status, d_stats,
+                       s->counters + 0, s->redo, s->counters + 2, nullptr, nullptr, mixed, grid1, s->cta, st);
   if (rc) return rc;
   if (mixed) {
-    // cells whose FP32 Newton iteration failed are re-solved in FP64
-    rc = launch_chem_warp(net, ncell, d_abundance, d_rate, d_density, d_t_end_yr, o, d_status, d_stats,
-                          s->counters + 1, nullptr, nullptr, s->redo, s->counters + 2, false, sms, st);
+    rc = launch_chem_cta(net, ncell, d_abundance, d_rate, d_density, d_t_end_yr, o, d_status, d_stats,
+                         s->counters + 1, nullptr, nullptr, s->redo, s->counters + 2, false, grid2, s->cta, st);
     if (rc) return rc;
   }
   return 0;
@@ -234,11 +298,16 @@ int pdr_chem_autotune(const pdr_net *net, int ncell_sample, const double *d_abun
   cudaEventCreate(&t0);
   cudaEventCreate(&t1);
   struct Cand { int wpb, reg, refill; };
-  const Cand cands[] = {{4, 0, 0}, {2, 0, 0}, {8, 0, 0}, {4, 1, 0}, {8, 1, 0}, {4, 0, 1}};
+  const Cand warp_cands[] = {{4, 0, 0}, {2, 0, 0}, {8, 0, 0}, {4, 1, 0}, {8, 1, 0}, {4, 0, 1}};
+  const Cand cta_cands[] = {{0, 0, 0}, {0, 0, 1}};   // block integrator: work queue or static refill
+  const bool warp_path = (opts->integrator == 1) || (opts->integrator == 0 && net->warp_ok && net->host.neq == 32);
+  const Cand *cands = warp_path ? warp_cands : cta_cands;
+  const int ncand = warp_path ? 6 : 2;
   float best = 1e30f;
   pdr_chem_opts best_o = *opts;
   int rc = 0;
-  for (const Cand &c : cands) {
+  for (int ci = 0; ci < ncand; ci++) {
+    const Cand &c = cands[ci];
     pdr_chem_opts o = *opts;
     o.warps_per_block = c.wpb;
     o.reg_variant = c.reg;

@@ -1,0 +1,644 @@
+// chem_cta.cu -- batched BDF chemistry integrator, one thread block per cell.
+//
+// Replaces the per-cell CVODE solve of calculate_abundances.c:124-326 for
+// networks of any size up to 252 ODE species (the full network has 214, the
+// "mynetwork" example 57).  The block has G = 32*ceil(neq/32) threads (at
+// least 64); thread i owns species i: its Nordsieck row, error weight and
+// correction, and row i of the Newton matrix.  The CVODE control logic is the
+// one shared with the warp-per-cell integrator (bdf_core.cuh); this file
+// supplies the block-wide collectives, the network RHS and Jacobian, and the
+// dense linear algebra:
+//
+//   RHS  fluxes phi_r = kn_r x_a x_b reaction-parallel over the block, the
+//        stoichiometric sums in G balanced chunks with deterministic partial
+//        sums (the same scheme as the warp integrator, stride G);
+//   Jac  thread i accumulates row i from its term list, then the x_e chain
+//        rule J_ij += (df_i/dx_e) c_j;
+//   LU   dense LU with partial pivoting (CVDense semantics: in each column the
+//        unpivoted row of largest magnitude, lowest row on ties), rows kept in
+//        place with the pivot order recorded; right-looking in panels of 8
+//        columns: per panel the pivot rows' U block is formed column-parallel
+//        and the trailing update is a rank-8 update applied by the row owners;
+//   solve forward/backward substitution in 32-row blocks: the 32x32 diagonal
+//        blocks of L and U are inverted in place at setup, so a block step is
+//        a 32x32 product by one warp plus a rank-32 update by the row owners.
+//
+// The matrix is column-major, element (i, j) at j*ld + i with ld odd: thread
+// i's accesses to its own row are consecutive across a warp (coalesced in
+// global memory, conflict-free in shared memory) and the pivot-row reads are
+// broadcasts.  PDR_MIXED keeps it in shared memory in FP32 after the
+// similarity scaling W M W^-1, W = diag(1/(rtol|y|+atol)) (the full network's
+// 214 x 216 FP32 matrix plus the integrator's arrays fit the 227 KB of one
+// block); PDR_FP64 keeps it in FP64, in shared memory when it fits and
+// otherwise in a per-block slot of global memory that stays in L2.  A cell
+// whose FP32 Newton iteration fails with a fresh matrix is re-solved in FP64.
+#include <cstdint>
+#include <mutex>
+#include <type_traits>
+
+#include "bdf_core.cuh"
+#include "pdr_internal.h"
+
+namespace pdr {
+
+namespace {
+
+using namespace bdf;
+constexpr unsigned FULL = 0xffffffffu;
+constexpr int PB = 8;    // LU panel width
+constexpr int DB = 32;   // diagonal block of the triangular solves
+constexpr int MAXW = 8;  // at most 256 threads per block
+
+struct CtaArgs {
+  WarpTables tab;
+  int ncell, nspec, nreac, n, ld, G;
+  double *abundance;
+  const double *rate;
+  const double *density;
+  const double *t_end_yr;
+  double t_end_default_yr, start_time_yr, reltol, abstol;
+  long long mxstep, max_total_steps;
+  int *status;
+  int *stats;
+  const int *cell_list;
+  int *queue;
+  int *fallback_list;
+  int *fallback_count;
+  int refill_static;
+  double *kn_global;      // [gridDim.x][nreac] rate constants (times n_H where the RHS has it)
+  void *mat_global;       // [gridDim.x][(n+2)*ld] Newton matrix, when it is not in shared memory
+};
+
+// byte offsets of the block's shared arrays (host and device agree)
+struct CtaLayout {
+  size_t scr, xs, part, red, sig, perm, bsv, ys, upan, ws, mat, total;
+};
+
+__host__ __device__ inline size_t al16(size_t x) { return (x + 15) & ~size_t(15); }
+
+__host__ __device__ inline CtaLayout cta_layout(int n, int nreac, int nparts, int G, int ld, size_t mt,
+                                                bool mat_smem) {
+  CtaLayout L;
+  size_t o = 0;
+  const size_t scr = (size_t)nreac * (8 > 2 * mt ? 8 : 2 * mt);
+  L.scr = o; o += al16(scr);
+  L.xs = o; o += al16(8 * (size_t)(n + 2));
+  L.part = o; o += al16(8 * (size_t)(nparts + 1));
+  L.red = o; o += al16(2 * MAXW * (8 + 8 + 4));   // sums, argmax keys, argmax rows
+  L.sig = o; o += al16(4 * (size_t)(n + 2));
+  L.perm = o; o += al16(4 * (size_t)n);
+  L.bsv = o; o += al16(mt * (size_t)G);
+  L.ys = o; o += al16(mt * (size_t)(n + DB));
+  L.upan = o; o += al16(mt * PB * (size_t)n);
+  L.ws = o; o += al16(sizeof(CoefShared));
+  L.mat = o;
+  if (mat_smem) o += al16(mt * (size_t)(n + 2) * ld);
+  L.total = o;
+  return L;
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+  return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(FULL, v, o));
+  return v;
+}
+
+// ordering key of a non-negative magnitude (0 = not a candidate)
+__device__ __forceinline__ unsigned long long mag_key(float v, bool cand) {
+  return cand ? (unsigned long long)__float_as_uint(v) : 0ull;
+}
+__device__ __forceinline__ unsigned long long mag_key(double v, bool cand) {
+  return cand ? (unsigned long long)__double_as_longlong(v) : 0ull;
+}
+
+template <bool MIXED>
+struct CtaCell : Core<CtaCell<MIXED>> {
+  using MT = typename std::conditional<MIXED, float, double>::type;
+  const CtaArgs &A;
+  const int tid, lane, warp, nw, n, ld;
+  const bool owns;
+  const double inv_n;
+  double *kn;            // global, this block's slot
+  double *scr, *xs, *part;
+  double *red_d;         // [2][MAXW] reduction partials
+  unsigned long long *red_k;  // [2][MAXW] argmax keys
+  int *red_i;            // [2][MAXW] argmax rows
+  float *sig;
+  int *perm;
+  MT *bsv, *ys, *upan, *mat;
+  int rbuf = 0;          // alternating reduction buffer
+  double cx;
+  int mystep;
+  double wsc, ssc;
+
+  __device__ __forceinline__ CtaCell(const CtaArgs &a, int t)
+      : A(a), tid(t), lane(t & 31), warp(t >> 5), nw(blockDim.x >> 5), n(a.n), ld(a.ld), owns(t < a.n),
+        inv_n(1.0 / a.n) {}
+
+  __device__ __forceinline__ bool leader() const { return tid == 0; }
+  __device__ __forceinline__ void sync() const { __syncthreads(); }
+  __device__ __forceinline__ MT &M(int i, int j) const { return mat[(size_t)j * ld + i]; }
+
+  // block-wide sums and maxima in a fixed order (every thread gets the value)
+  __device__ __forceinline__ double sum_all(double v) {
+    v = warp_sum(v);
+    double *r = red_d + rbuf * MAXW;
+    rbuf ^= 1;
+    if (lane == 0) r[warp] = v;
+    __syncthreads();
+    double s = 0.0;
+    for (int w = 0; w < nw; w++) s += r[w];
+    return s;
+  }
+  __device__ __forceinline__ double max_all(double v) {
+    v = warp_max(v);
+    double *r = red_d + rbuf * MAXW;
+    rbuf ^= 1;
+    if (lane == 0) r[warp] = v;
+    __syncthreads();
+    double s = r[0];
+    for (int w = 1; w < nw; w++) s = fmax(s, r[w]);
+    return s;
+  }
+  // row of the largest candidate (lowest row on ties), -1 if all are zero
+  __device__ __forceinline__ int argmax_all(MT v, bool cand) {
+    const unsigned long long key = mag_key(v, cand);
+    const unsigned hi = (unsigned)(key >> 32), lo = (unsigned)key;
+    const unsigned mh = __reduce_max_sync(FULL, hi);
+    const unsigned ml = __reduce_max_sync(FULL, hi == mh ? lo : 0u);
+    const unsigned b = __ballot_sync(FULL, cand && hi == mh && lo == ml);
+    unsigned long long *rk = red_k + rbuf * MAXW;
+    int *ri = red_i + rbuf * MAXW;
+    rbuf ^= 1;
+    if (lane == 0) {
+      rk[warp] = ((unsigned long long)mh << 32) | ml;
+      ri[warp] = b ? warp * 32 + __ffs(b) - 1 : -1;
+    }
+    __syncthreads();
+    unsigned long long best = 0ull;
+    int row = -1;
+    for (int w = 0; w < nw; w++)
+      if (rk[w] > best) { best = rk[w]; row = ri[w]; }
+    return row;
+  }
+
+  __device__ __forceinline__ double slot_value(int s, double xe) const { return s == n ? xe : xs[s]; }
+
+  // f(y): returns f of this thread's species, records x_e of this call
+  __device__ __forceinline__ double rhs(double yv) {
+    const WarpTables &T = A.tab;
+    const int G = T.lanes;
+    if (owns) xs[tid] = yv;
+    const double xe = sum_all(owns ? cx * yv : 0.0);
+    this->xe_last = xe;
+    for (int r = tid; r < T.nreac; r += G) {
+      const int2 ab = __ldg(&T.rab[r]);
+      scr[r] = kn[r] * slot_value(ab.x, xe) * slot_value(ab.y, xe);
+    }
+    __syncthreads();
+    double s = 0.0;
+#pragma unroll 4
+    for (int t = 0; t < T.rhs_len; t++) {
+      const int rf = __ldg(&T.rhs_rf[t * G + tid]);
+      const double nu = __ldg(&T.rhs_nu[t * G + tid]);
+      s = fma(nu, scr[rf & 0xffff], s);
+      const int fl = (rf >> 16) - 1;
+      if (fl >= 0) { part[fl] = s; s = 0.0; }
+    }
+    __syncthreads();
+    double f = 0.0;
+    for (int k = 0; k < T.plist_len; k++) f += part[__ldg(&T.plist[k * G + tid])];
+    this->nfe++;
+    return owns ? f : 0.0;
+  }
+
+  // Newton matrix rows: FP64 M = I - gamma J; mixed FP32 W M W^-1
+  __device__ __forceinline__ void assemble(double yv, double rf_d) {
+    const WarpTables &T = A.tab;
+    const int G = T.lanes;
+    if (owns) xs[tid] = yv;
+    if constexpr (MIXED) {
+      ssc = this->rtol * fabs(yv) + this->atol;
+      wsc = 1.0 / ssc;
+      if (owns) sig[tid] = (float)(ssc / this->atol);
+    }
+    const double xe = sum_all(owns ? cx * yv : 0.0);
+    MT *Da = reinterpret_cast<MT *>(scr);
+    MT *Db = Da + T.nreac;
+    for (int r = tid; r < T.nreac; r += G) {
+      const int2 ab = __ldg(&T.rab[r]);
+      const double k = kn[r];
+      if constexpr (MIXED) {
+        Da[r] = (float)(k * slot_value(ab.y, xe)) * sig[ab.x];
+        Db[r] = (float)(k * slot_value(ab.x, xe)) * sig[ab.y];
+      } else {
+        Da[r] = k * slot_value(ab.y, xe);
+        Db[r] = (ab.y == n + 1) ? 0.0 : k * slot_value(ab.x, xe);
+      }
+    }
+    if (owns)
+      for (int j = 0; j < n + 2; j++) M(tid, j) = MT(0);
+    __syncthreads();
+    if (owns) {
+      for (int t = 0; t < T.jac_len; t++) {
+        MT nu;
+        if constexpr (MIXED) nu = __ldg(&T.jac_nu_f[t * G + tid]);
+        else nu = __ldg(&T.jac_nu[t * G + tid]);
+        if (nu == MT(0)) break;
+        const int rab = __ldg(&T.jac_rab[t * G + tid]);
+        const int r = rab & 0xffff, a = (rab >> 16) & 0xff, b = (rab >> 24) & 0xff;
+        M(tid, a) = fma(nu, Da[r], M(tid, a));
+        M(tid, b) = fma(nu, Db[r], M(tid, b));
+      }
+      const MT e = M(tid, n);
+      MT rf;
+      if constexpr (MIXED) rf = (MT)(rf_d * (wsc * this->atol));
+      else rf = (MT)rf_d;
+      for (int j = 0; j < n; j++) {
+        const MT cj = (MT)__ldg(&T.xe_coef[j]);
+        MT v = M(tid, j);
+        if constexpr (MIXED) v = fmaf(e * cj, sig[j], v);
+        else v = fma(e, cj, v);
+        M(tid, j) = rf * v + (tid == j ? MT(1) : MT(0));
+      }
+    }
+  }
+
+  __device__ __forceinline__ MT rcp(MT x) const {
+    if constexpr (sizeof(MT) == 8) return __drcp_rn(x);
+    else return __frcp_rn(x);
+  }
+
+  // LU with partial pivoting in place; false if a column has no nonzero pivot
+  __device__ __forceinline__ bool lu() {
+    mystep = owns ? -1 : n;
+    for (int k0 = 0; k0 < n; k0 += PB) {
+      const int kb = min(PB, n - k0);
+      for (int t = 0; t < kb; t++) {
+        const int k = k0 + t;
+        const bool cand = (mystep < 0);
+        const int p = argmax_all(cand ? (MT)fabs(M(tid, k)) : MT(0), cand);
+        if (p < 0) return false;
+        const MT rinv = rcp(M(p, k));
+        if (tid == p) { mystep = k; perm[k] = p; }
+        if (mystep < 0) {
+          const MT l = M(tid, k) * rinv;
+          M(tid, k) = l;
+          for (int j = k + 1; j < k0 + kb; j++) M(tid, j) = fma(-l, M(p, j), M(tid, j));
+        }
+      }
+      __syncthreads();
+      // U rows of this panel's pivots, columns right of the panel
+      for (int j = k0 + kb + tid; j < n; j += blockDim.x) {
+        MT u[PB];
+#pragma unroll
+        for (int t = 0; t < PB; t++) {
+          if (t < kb) {
+            const int pt = perm[k0 + t];
+            MT s = M(pt, j);
+#pragma unroll
+            for (int t2 = 0; t2 < PB; t2++)
+              if (t2 < t) s = fma(-M(pt, k0 + t2), u[t2], s);
+            u[t] = s;
+            M(pt, j) = s;
+          } else {
+            u[t] = MT(0);
+          }
+          upan[(size_t)j * PB + t] = u[t];
+        }
+      }
+      __syncthreads();
+      if (mystep < 0) {
+        MT l[PB];
+#pragma unroll
+        for (int t = 0; t < PB; t++) l[t] = (t < kb) ? M(tid, k0 + t) : MT(0);
+        for (int j = k0 + kb; j < n; j++) {
+          MT s = M(tid, j);
+#pragma unroll
+          for (int t = 0; t < PB; t++) s = fma(-l[t], upan[(size_t)j * PB + t], s);
+          M(tid, j) = s;
+        }
+      }
+    }
+    __syncthreads();
+    return true;
+  }
+
+  // invert the 32x32 diagonal blocks of L (unit lower) and U in place
+  __device__ __forceinline__ void invert_diagonal_blocks() {
+    const int nb = (n + DB - 1) / DB;
+    for (int c = warp; c < nb; c += nw) {
+      const int k0 = c * DB, bs = min(DB, n - k0);
+      const int t = lane;  // column of the block
+      MT x[DB];
+      // L^-1 column t: x_t = 1, x_r = -sum_{m=t}^{r-1} L_rm x_m
+#pragma unroll
+      for (int r = 0; r < DB; r++) {
+        if (r < bs) {
+          const int pr = perm[k0 + r];
+          MT s = MT(0);
+#pragma unroll
+          for (int m = 0; m < DB; m++)
+            if (m < r && m >= t) s = fma(-M(pr, k0 + m), x[m], s);
+          x[r] = (r == t) ? MT(1) : (r > t ? s : MT(0));
+        } else {
+          x[r] = MT(0);
+        }
+      }
+      __syncwarp();
+#pragma unroll
+      for (int r = 0; r < DB; r++)
+        if (r < bs && t < bs && r > t) M(perm[k0 + r], k0 + t) = x[r];
+      __syncwarp();
+      // U^-1 column t: y_t = 1/U_tt, y_r = -(sum_{m=r+1}^{t} U_rm y_m) / U_rr
+#pragma unroll
+      for (int r = DB - 1; r >= 0; r--) {
+        if (r < bs) {
+          const int pr = perm[k0 + r];
+          MT s = MT(0);
+#pragma unroll
+          for (int m = 0; m < DB; m++)
+            if (m > r && m <= t && m < bs) s = fma(M(pr, k0 + m), x[m], s);
+          const MT d = rcp(M(pr, k0 + r));
+          x[r] = (r == t) ? d : (r < t ? -s * d : MT(0));
+        } else {
+          x[r] = MT(0);
+        }
+      }
+      __syncwarp();
+#pragma unroll
+      for (int r = 0; r < DB; r++)
+        if (r < bs && t < bs && r <= t) M(perm[k0 + r], k0 + t) = x[r];
+    }
+    __syncthreads();
+  }
+
+  __device__ __forceinline__ bool setup(double yv) {
+    assemble(yv, -this->gamma);
+    bool ok = lu();
+    if (ok) {
+      // any non-finite factor entry fails the setup (as a singular matrix)
+      bool finite = true;
+      if (owns)
+        for (int j = 0; j < n; j++) finite &= isfinite(M(tid, j));
+      ok = __syncthreads_and(finite);
+    }
+    if (ok) invert_diagonal_blocks();
+    this->after_setup();
+    return ok;
+  }
+
+  // x = M^-1 b for this thread's component
+  __device__ __forceinline__ double solve(double b) {
+    const int nb = (n + DB - 1) / DB;
+    MT v;
+    if constexpr (MIXED) v = owns ? (MT)(b * wsc) : MT(0);
+    else v = owns ? (MT)b : MT(0);
+    bsv[tid] = v;
+    __syncthreads();
+    // forward: L y = P b
+    for (int c = 0; c < nb; c++) {
+      const int k0 = c * DB, bs = min(DB, n - k0);
+      if (warp == c % nw) {
+        const int pr = (lane < bs) ? perm[k0 + lane] : 0;
+        const MT s = (lane < bs) ? bsv[pr] : MT(0);
+        MT y = s;
+#pragma unroll
+        for (int t = 0; t < DB; t++) {
+          const MT st = __shfl_sync(FULL, s, t);
+          if (t < lane && lane < bs) y = fma(M(pr, k0 + t), st, y);
+        }
+        if (lane < bs) ys[k0 + lane] = y;
+      }
+      __syncthreads();
+      if (mystep >= k0 + bs && owns) {
+        MT s = v;
+        for (int t = 0; t < bs; t++) s = fma(-M(tid, k0 + t), ys[k0 + t], s);
+        v = s;
+        bsv[tid] = v;
+      }
+      __syncthreads();
+    }
+    // backward: U x = y; the running value of logical row k is kept by its pivot row
+    v = owns ? ys[mystep] : MT(0);
+    bsv[tid] = v;
+    __syncthreads();
+    for (int c = nb - 1; c >= 0; c--) {
+      const int k0 = c * DB, bs = min(DB, n - k0);
+      if (warp == c % nw) {
+        // x_r = sum_{t>=r} Uinv_rt s_t, s_t the running value of logical row k0+t
+        const int pr = (lane < bs) ? perm[k0 + lane] : 0;
+        const MT s = (lane < bs) ? bsv[pr] : MT(0);
+        MT x = MT(0);
+#pragma unroll
+        for (int t = 0; t < DB; t++) {
+          const MT st = __shfl_sync(FULL, s, t);
+          if (t >= lane && lane < bs && t < bs) x = fma(M(pr, k0 + t), st, x);
+        }
+        if (lane < bs) ys[k0 + lane] = x;
+      }
+      __syncthreads();
+      if (owns && mystep < k0) {
+        MT s = v;
+        for (int t = 0; t < bs; t++) s = fma(-M(tid, k0 + t), ys[k0 + t], s);
+        v = s;
+        bsv[tid] = v;
+      }
+      __syncthreads();
+    }
+    // ys[k] is now the solution component of column k = species k
+    const MT xv = owns ? ys[tid] : MT(0);
+    __syncthreads();
+    if constexpr (MIXED) return owns ? (double)xv * ssc : 0.0;
+    else return owns ? (double)xv : 0.0;
+  }
+
+  // calculate_abundances.c:132-317 for one cell
+  __device__ __forceinline__ void run(int cell) {
+    const int nspec = A.nspec;
+    double *ab = A.abundance + (size_t)cell * nspec;
+    const double n_H = A.density[cell];
+    this->rtol = A.reltol;
+    this->atol = A.abstol;
+    this->mxstep = A.mxstep;
+    this->max_total_steps = A.max_total_steps;
+    cx = owns ? __ldg(&A.tab.xe_coef[tid]) : 0.0;
+    const double *rate = A.rate + (size_t)cell * A.nreac;
+    for (int r = tid; r < A.nreac; r += blockDim.x)
+      kn[r] = __ldg(&rate[r]) * (__ldg(&A.tab.nh_mask[r]) != 0.0 ? n_H : 1.0);
+    if (tid == 0) {
+      xs[n + 1] = 1.0;
+      part[A.tab.nparts] = 0.0;
+      sig[n] = 1.0f;
+      sig[n + 1] = 0.0f;
+    }
+#pragma unroll
+    for (int j = 0; j <= QMAX; j++) this->z[j] = 0.0;
+    this->z[0] = owns ? ab[tid] : 0.0;
+    this->xe_last = ab[nspec - 1];
+    __syncthreads();
+    const double tend_yr = A.t_end_yr ? A.t_end_yr[cell] : A.t_end_default_yr;
+    double yv = 0.0;
+    const int status = this->integrate(A.start_time_yr, tend_yr, MIXED, &yv);
+    if (status == FELL_BACK) {
+      if (tid == 0) {
+        const int k = atomicAdd(A.fallback_count, 1);
+        A.fallback_list[k] = cell;
+        A.status[cell] = FELL_BACK;
+      }
+      return;
+    }
+    if (yv < this->atol) yv = 0.0;
+    if (owns) ab[tid] = yv;
+    if (tid == 0) {
+      ab[nspec - 1] = this->xe_last;
+      A.status[cell] = status;
+      if (A.stats) {
+        int *s = A.stats + (size_t)cell * 8;
+        s[0] = this->nst; s[1] = this->nfe; s[2] = this->nje; s[3] = this->nsetups;
+        s[4] = this->nni; s[5] = this->ncfn; s[6] = this->netf; s[7] = MIXED ? 0 : (A.cell_list ? 1 : 0);
+      }
+    }
+  }
+};
+
+template <bool MIXED>
+__global__ void __launch_bounds__(256, 1) chem_cta_kernel(const __grid_constant__ CtaArgs A, int total_cells,
+                                                          const int *total_ptr, int mat_smem) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  using MT = typename std::conditional<MIXED, float, double>::type;
+  const CtaLayout L = cta_layout(A.n, A.nreac, A.tab.nparts, A.G, A.ld, sizeof(MT), mat_smem != 0);
+  CtaCell<MIXED> c(A, threadIdx.x);
+  c.kn = A.kn_global + (size_t)blockIdx.x * A.nreac;
+  c.scr = reinterpret_cast<double *>(smem_raw + L.scr);
+  c.xs = reinterpret_cast<double *>(smem_raw + L.xs);
+  c.part = reinterpret_cast<double *>(smem_raw + L.part);
+  c.red_d = reinterpret_cast<double *>(smem_raw + L.red);
+  c.red_k = reinterpret_cast<unsigned long long *>(smem_raw + L.red + 2 * MAXW * 8);
+  c.red_i = reinterpret_cast<int *>(smem_raw + L.red + 2 * MAXW * 16);
+  c.sig = reinterpret_cast<float *>(smem_raw + L.sig);
+  c.perm = reinterpret_cast<int *>(smem_raw + L.perm);
+  c.bsv = reinterpret_cast<MT *>(smem_raw + L.bsv);
+  c.ys = reinterpret_cast<MT *>(smem_raw + L.ys);
+  c.upan = reinterpret_cast<MT *>(smem_raw + L.upan);
+  c.ws = reinterpret_cast<CoefShared *>(smem_raw + L.ws);
+  c.mat = mat_smem ? reinterpret_cast<MT *>(smem_raw + L.mat)
+                   : reinterpret_cast<MT *>(A.mat_global) + (size_t)blockIdx.x * (A.n + 2) * A.ld;
+  c.build_uniform_table();
+  if (total_ptr) total_cells = *total_ptr;
+  __shared__ int next_idx;
+  for (int k = 0;; k++) {
+    int idx;
+    if (A.refill_static) {
+      idx = blockIdx.x + k * gridDim.x;
+    } else {
+      if (threadIdx.x == 0) next_idx = atomicAdd(A.queue, 1);
+      __syncthreads();
+      idx = next_idx;
+      __syncthreads();
+    }
+    if (idx >= total_cells) break;
+    const int cell = A.cell_list ? A.cell_list[idx] : idx;
+    c.run(cell);
+    __syncthreads();
+  }
+}
+
+}  // namespace
+
+// shared memory of one block, and whether the matrix is in it
+size_t chem_cta_smem(const pdr_net *net, bool mixed, bool *mat_smem) {
+  const WarpTables &T = net->cta;
+  const int n = T.neq, ld = n | 1;
+  const size_t mt = mixed ? 4 : 8;
+  CtaLayout with = cta_layout(n, T.nreac, T.nparts, T.lanes, ld, mt, true);
+  int dev = 0, optin = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (with.total + 64 <= (size_t)optin) { *mat_smem = true; return with.total; }   // + static shared
+  *mat_smem = false;
+  return cta_layout(n, T.nreac, T.nparts, T.lanes, ld, mt, false).total;
+}
+
+// Per-launch global scratch of the block integrator: rate constants and, when
+// the matrix does not fit shared memory, the matrix, one slot per block.
+size_t chem_cta_global_bytes(const pdr_net *net, bool mixed, int grid) {
+  bool ms = false;
+  chem_cta_smem(net, mixed, &ms);
+  const WarpTables &T = net->cta;
+  const int n = T.neq, ld = n | 1;
+  size_t b = al16((size_t)grid * T.nreac * 8);
+  if (!ms) b += al16((size_t)grid * (n + 2) * ld * (mixed ? 4 : 8));
+  return b;
+}
+
+// blocks per SM the block integrator runs with (0 on error)
+int chem_cta_blocks_per_sm(const pdr_net *net, bool mixed) {
+  bool ms = false;
+  const size_t smem = chem_cta_smem(net, mixed, &ms);
+  auto k = mixed ? chem_cta_kernel<true> : chem_cta_kernel<false>;
+  if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, net->cta.lanes, smem) != cudaSuccess) return 0;
+  return per_sm;
+}
+
+// Launch the persistent block integrator over `ncell` cells (or the listed
+// ones) with `grid` blocks; `scratch` holds chem_cta_global_bytes(grid) bytes.
+int launch_chem_cta(const pdr_net *net, int ncell, double *ab, const double *rate, const double *dens,
+                    const double *tend, const pdr_chem_opts &o, int *status, int *stats, int *queue,
+                    int *fb_list, int *fb_count, const int *cell_list, const int *total_ptr, bool mixed,
+                    int grid, void *scratch, cudaStream_t st) {
+  const WarpTables &T = net->cta;
+  if (!net->cta_ok || T.lanes > 256) return PDR_E_NET;
+  CtaArgs A;
+  A.tab = T;
+  A.ncell = ncell;
+  A.nspec = net->host.nspec;
+  A.nreac = net->host.nreac;
+  A.n = T.neq;
+  A.ld = T.neq | 1;
+  A.G = T.lanes;
+  A.abundance = ab;
+  A.rate = rate;
+  A.density = dens;
+  A.t_end_yr = tend;
+  A.t_end_default_yr = o.end_time_yr;
+  A.start_time_yr = o.start_time_yr;
+  A.reltol = o.reltol;
+  A.abstol = o.abstol;
+  A.mxstep = o.mxstep;
+  A.max_total_steps = 500000;
+  A.status = status;
+  A.stats = stats;
+  A.cell_list = cell_list;
+  A.queue = queue;
+  A.fallback_list = fb_list;
+  A.fallback_count = fb_count;
+  A.refill_static = (o.refill == 1) ? 1 : 0;
+  bool ms = false;
+  const size_t smem = chem_cta_smem(net, mixed, &ms);
+  A.kn_global = reinterpret_cast<double *>(scratch);
+  A.mat_global = ms ? nullptr : reinterpret_cast<unsigned char *>(scratch) + al16((size_t)grid * T.nreac * 8);
+  auto k = mixed ? chem_cta_kernel<true> : chem_cta_kernel<false>;
+  static std::mutex mu;
+  static size_t cached[2] = {0, 0};
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    if (cached[mixed] != smem) {
+      cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(chem_cta_kernel)");
+      cached[mixed] = smem;
+    }
+  }
+  k<<<grid, T.lanes, smem, st>>>(A, ncell, total_ptr, ms ? 1 : 0);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? 0 : cuda_fail(e, "chem_cta_kernel launch");
+}
+
+}  // namespace pdr

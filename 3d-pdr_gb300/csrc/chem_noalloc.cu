@@ -83,8 +83,10 @@ extern "C" int pdr_chem_solve_batched_noalloc(const pdr_net *net, int ncell, dou
     set_error("pdr_chem_solve_batched_noalloc: invalid options");
     return PDR_E_ARG;
   }
-  if (!net->warp_ok || net->host.neq != 32) {
-    set_error("pdr_chem_solve_batched_noalloc: this build integrates networks with 32 ODE species");
+  if (!net->warp_ok || net->host.neq != 32 || o.integrator == 2) {
+    // the block integrator needs per-block scratch that scales with the grid
+    set_error("pdr_chem_solve_batched_noalloc: only the warp integrator (networks of 32 ODE species) "
+              "runs without allocation");
     return PDR_E_NET;
   }
   int dev = 0, sms = 0;

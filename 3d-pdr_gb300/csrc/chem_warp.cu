@@ -92,60 +92,58 @@ __device__ __forceinline__ int argmax_lane(double v, bool cand) {
   return (mh == 0u && ml == 0u) ? -1 : __ffs(b) - 1;
 }
 
-// In-register LU with partial pivoting, lane = row.  m[] holds row `lane`;
-// on exit m[j<step] are the multipliers, m[j>=step] the U row, mystep the
-// elimination step at which this row was the pivot, invd 1/diagonal.
+// LU with partial pivoting of the rows held in shared memory, lane i = row i
+// at a + i*ld.  Rows stay in place: on exit row i holds its multipliers in
+// the columns before the step at which it was the pivot (mystep) and its U
+// row from there on; invd = 1/diagonal, perm[k] = pivot row of step k.  (A
+// register-resident row would need the nest fully unrolled and kept the
+// integrator's state out of registers.)
 template <int N, class MT>
-__device__ __forceinline__ bool lu_rows(MT (&m)[N], int lane, int &mystep, MT &invd, int *perm) {
+__device__ __forceinline__ bool lu_rows(MT *a, int ld, int lane, int &mystep, MT &invd, int *perm) {
   mystep = (lane < N) ? -1 : N;
-#pragma unroll
+  MT *row = a + lane * ld;
   for (int k = 0; k < N; k++) {
     const bool cand = (mystep < 0);
-    const int p = argmax_lane(cand ? fabs(m[k]) : MT(0), cand);
+    const int p = argmax_lane(cand ? fabs(row[k]) : MT(0), cand);
     if (p < 0) return false;
-    const MT u = bcast(m[k], p);
+    const MT *prow = a + p * ld;
     MT rinv;
-    if constexpr (sizeof(MT) == 8) rinv = __drcp_rn(u);
-    else rinv = __frcp_rn(u);
+    if constexpr (sizeof(MT) == 8) rinv = __drcp_rn(prow[k]);
+    else rinv = __frcp_rn(prow[k]);
     if (lane == p) { mystep = k; invd = rinv; perm[k] = p; }
-    const bool upd = (mystep < 0);
-    const MT l = m[k] * rinv;
-    if (upd) m[k] = l;
-#pragma unroll
-    for (int j = k + 1; j < N; j++) {
-      const MT pv = bcast(m[j], p);
-      if (upd) m[j] = fma(-l, pv, m[j]);
+    if (mystep < 0) {
+      const MT l = row[k] * rinv;
+      row[k] = l;
+      for (int j = k + 1; j < N; j++) row[j] = fma(-l, prow[j], row[j]);
     }
+    __syncwarp();
   }
   return true;
 }
 
 // Solve with the row-distributed LU: b is this lane's right-hand-side entry
-// (row `lane`), the solution component for column `lane` is returned;
-// perm[k] is the lane that was the pivot row of step k.
+// (row `lane`), the solution component for column `lane` is returned.
 template <int N, class MT>
-__device__ __forceinline__ MT lu_solve_rows(const MT (&m)[N], int lane, int mystep, MT invd, MT b,
+__device__ __forceinline__ MT lu_solve_rows(const MT *a, int ld, int lane, int mystep, MT invd, MT b,
                                             const int *perm) {
-#pragma unroll
+  const MT *row = a + (lane < N ? lane : 0) * ld;
   for (int k = 0; k < N; k++) {
-    const int p = perm[k];
-    const MT yk = bcast(b, p);
-    if (mystep > k) b = fma(-m[k], yk, b);
+    const MT yk = bcast(b, perm[k]);
+    if (mystep > k) b = fma(-row[k], yk, b);
   }
   MT x = MT(0);
-#pragma unroll
   for (int k = N - 1; k >= 0; k--) {
-    const int p = perm[k];
-    const MT xk = bcast(b * invd, p);
+    const MT xk = bcast(b * invd, perm[k]);
     if (lane == k) x = xk;
-    if (mystep < k) b = fma(-m[k], xk, b);
+    if (mystep < k) b = fma(-row[k], xk, b);
   }
   return x;
 }
 
 // One cell integrated by one warp: lane = species = Newton-matrix row.
-template <int NSP, bool MIXED>
-struct WarpCell : Core<WarpCell<NSP, MIXED>> {
+// ZSH: Nordsieck rows in shared memory instead of registers.
+template <int NSP, bool MIXED, bool ZSH>
+struct WarpCell : Core<WarpCell<NSP, MIXED, ZSH>, ZSH> {
   using MT = typename std::conditional<MIXED, float, double>::type;
   const ChemArgs &A;
   const int lane;
@@ -153,11 +151,10 @@ struct WarpCell : Core<WarpCell<NSP, MIXED>> {
   const double inv_n = 1.0 / NSP;
   // shared-memory views of this warp
   double *kn, *scr, *xs, *part;
-  MT *jrow;       // [NSP][NSP+3]
+  MT *jrow;       // [NSP][NSP+3] Newton matrix rows / their LU factors
   float *sig;     // [NSP+2] column scales (mixed)
   int *perm;      // [NSP] pivot lane of each elimination step
   double cx;      // electron-sum coefficient of species `lane`
-  MT m[NSP];      // row `lane` of the Newton matrix / its LU factors
   int mystep;
   MT invd;
   double wsc, ssc;   // setup-time weight and its inverse (mixed scaling)
@@ -253,7 +250,7 @@ struct WarpCell : Core<WarpCell<NSP, MIXED>> {
       MT v = owns ? row[j] : MT(0);
       if constexpr (MIXED) v = fmaf(e * cj, sig[j], v);
       else v = fma(e, cj, v);
-      m[j] = rf * v + ((identity && lane == j) ? MT(1) : MT(0));
+      if (owns) row[j] = rf * v + ((identity && lane == j) ? MT(1) : MT(0));
     }
     __syncwarp();
   }
@@ -261,11 +258,12 @@ struct WarpCell : Core<WarpCell<NSP, MIXED>> {
   // Newton matrix at y: FP64 M = I - gamma J, or FP32 W M W^-1, factorised
   __device__ __forceinline__ bool setup(double yv) {
     assemble(yv, -this->gamma, true);
-    const bool ok = lu_rows<NSP, MT>(m, lane, mystep, invd, perm);
     __syncwarp();
+    const bool ok = lu_rows<NSP, MT>(jrow, NSP + 3, lane, mystep, invd, perm);
+    const MT *row = jrow + lane * (NSP + 3);
     bool finite = true;
-#pragma unroll
-    for (int j = 0; j < NSP; j++) finite &= isfinite(m[j]);
+    if (owns)
+      for (int j = 0; j < NSP; j++) finite &= isfinite(row[j]);
     finite = __all_sync(FULL, finite);
     this->after_setup();
     return ok && finite;
@@ -274,10 +272,10 @@ struct WarpCell : Core<WarpCell<NSP, MIXED>> {
   __device__ __forceinline__ double solve(double b) {
     double x;
     if constexpr (MIXED) {
-      const float xs_ = lu_solve_rows<NSP, float>(m, lane, mystep, invd, (float)(b * wsc), perm);
+      const float xs_ = lu_solve_rows<NSP, float>(jrow, NSP + 3, lane, mystep, invd, (float)(b * wsc), perm);
       x = (double)xs_ * ssc;
     } else {
-      x = lu_solve_rows<NSP, double>(m, lane, mystep, invd, b, perm);
+      x = lu_solve_rows<NSP, double>(jrow, NSP + 3, lane, mystep, invd, b, perm);
     }
     return owns ? x : 0.0;
   }
@@ -328,8 +326,9 @@ struct WarpCell : Core<WarpCell<NSP, MIXED>> {
   }
 };
 
-// MINB = 1 lets the compiler use up to ~160 registers per thread (12 warps/SM);
-// MINB = 2 caps them at 128 (16 warps/SM, some spills); the autotuner picks.
+// MINB = 1 lets the compiler use the registers it wants (8-12 warps/SM,
+// Nordsieck rows in registers); MINB = 2 caps them at 128 for 16 warps/SM
+// and keeps the Nordsieck rows in shared memory; the autotuner picks.
 template <int NSP, bool MIXED, int MINB>
 __global__ void __launch_bounds__(256, MINB) chem_warp_kernel(const __grid_constant__ ChemArgs A, int total_cells, const int *total_ptr) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -339,12 +338,13 @@ __global__ void __launch_bounds__(256, MINB) chem_warp_kernel(const __grid_const
   // per-warp shared layout
   const size_t kn_b = (size_t)nreac * 8, scr_b = (size_t)nreac * 16, xs_b = 8 * (NSP + 2);
   const size_t part_b = 8 * (A.tab.nparts + 1);
+  constexpr bool ZSH = (MINB >= 2);
   const size_t jrow_b = sizeof(MT) * NSP * (NSP + 3), sig_b = 4 * (NSP + 2) + 4 * NSP;
-  const size_t ws_b = sizeof(CoefShared);
+  const size_t ws_b = sizeof(CoefShared) + (ZSH ? 8 * (QMAX + 1) * kWarp : 0);
   auto al = [](size_t x) { return (x + 15) & ~size_t(15); };
   const size_t per_warp = al(kn_b) + al(scr_b) + al(xs_b) + al(part_b) + al(jrow_b) + al(sig_b) + al(ws_b);
   unsigned char *base = smem_raw + per_warp * warp;
-  WarpCell<NSP, MIXED> c(A, lane);
+  WarpCell<NSP, MIXED, ZSH> c(A, lane);
   c.kn = reinterpret_cast<double *>(base);
   c.scr = reinterpret_cast<double *>(base + al(kn_b));
   c.xs = reinterpret_cast<double *>(base + al(kn_b) + al(scr_b));
@@ -353,6 +353,10 @@ __global__ void __launch_bounds__(256, MINB) chem_warp_kernel(const __grid_const
   c.sig = reinterpret_cast<float *>(base + al(kn_b) + al(scr_b) + al(xs_b) + al(part_b) + al(jrow_b));
   c.perm = reinterpret_cast<int *>(c.sig + NSP + 2);
   c.ws = reinterpret_cast<CoefShared *>(base + al(kn_b) + al(scr_b) + al(xs_b) + al(part_b) + al(jrow_b) + al(sig_b));
+  if constexpr (ZSH) {
+    c.z.p = reinterpret_cast<double *>(reinterpret_cast<unsigned char *>(c.ws) + sizeof(CoefShared)) + lane;
+    c.z.s = kWarp;
+  }
   c.build_uniform_table();
   if (total_ptr) total_cells = *total_ptr;
   const int gwarp = blockIdx.x * (blockDim.x >> 5) + warp, nwarps = gridDim.x * (blockDim.x >> 5);
@@ -384,7 +388,7 @@ __global__ void __launch_bounds__(128) eval_kernel(const __grid_constant__ ChemA
   const size_t part_b = 8 * (A.tab.nparts + 1), jrow_b = 8 * NSP * (NSP + 3), sig_b = 4 * (NSP + 2) + 4 * NSP;
   const size_t per_warp = al(kn_b) + al(scr_b) + al(xs_b) + al(part_b) + al(jrow_b) + al(sig_b) + al(sizeof(CoefShared));
   unsigned char *base = smem_raw + per_warp * warp;
-  WarpCell<NSP, false> c(A, lane);
+  WarpCell<NSP, false, false> c(A, lane);
   c.kn = reinterpret_cast<double *>(base);
   c.scr = reinterpret_cast<double *>(base + al(kn_b));
   c.xs = reinterpret_cast<double *>(base + al(kn_b) + al(scr_b));
@@ -412,7 +416,7 @@ __global__ void __launch_bounds__(128) eval_kernel(const __grid_constant__ ChemA
       c.assemble(yv, 1.0, false);
       if (lane < NSP)
 #pragma unroll
-        for (int j = 0; j < NSP; j++) out[((size_t)s * NSP + lane) * NSP + j] = c.m[j];
+        for (int j = 0; j < NSP; j++) out[((size_t)s * NSP + lane) * NSP + j] = c.jrow[lane * (NSP + 3) + j];
     }
     __syncwarp();
   }
@@ -420,11 +424,12 @@ __global__ void __launch_bounds__(128) eval_kernel(const __grid_constant__ ChemA
 
 }  // namespace
 
-size_t chem_warp_smem_per_warp(int nsp, int nreac, int nparts, bool mixed) {
+size_t chem_warp_smem_per_warp(int nsp, int nreac, int nparts, bool mixed, bool zshared) {
   auto al = [](size_t x) { return (x + 15) & ~size_t(15); };
   const size_t mt = mixed ? 4 : 8;
   return al((size_t)nreac * 8) + al((size_t)nreac * 16) + al(8 * (nsp + 2)) + al(8 * (nparts + 1)) +
-         al(mt * nsp * (nsp + 3)) + al(4 * (nsp + 2) + 4 * nsp) + al(sizeof(CoefShared));
+         al(mt * nsp * (nsp + 3)) + al(4 * (nsp + 2) + 4 * nsp) +
+         al(sizeof(CoefShared) + (zshared ? 8 * (QMAX + 1) * kWarp : 0));
 }
 
 // Launch the persistent warp kernel over `ncell` cells (or the cells listed in
@@ -459,7 +464,7 @@ int launch_chem_warp(const pdr_net *net, int ncell, double *ab, const double *ra
   A.refill_static = (o.refill == 1) ? 1 : 0;
   const int wpb = o.warps_per_block > 0 ? o.warps_per_block : 4;
   if (wpb > 8) return PDR_E_ARG;
-  const size_t smem = chem_warp_smem_per_warp(32, A.nreac, T.nparts, mixed) * wpb;
+  const size_t smem = chem_warp_smem_per_warp(32, A.nreac, T.nparts, mixed, o.reg_variant == 1) * wpb;
   const int variant = (mixed ? 2 : 0) + (o.reg_variant == 1 ? 1 : 0);
   using KFn = void (*)(ChemArgs, int, const int *);
   static const KFn kernels[4] = {chem_warp_kernel<32, false, 1>, chem_warp_kernel<32, false, 2>,
@@ -504,7 +509,7 @@ int launch_chem_eval(const pdr_net *net, int nstate, const double *x, const doub
   A.density = dens;
   A.reltol = 1e-8;
   A.abstol = 1e-30;
-  const size_t smem = chem_warp_smem_per_warp(32, A.nreac, T.nparts, false) * 4;
+  const size_t smem = chem_warp_smem_per_warp(32, A.nreac, T.nparts, false, false) * 4;
   auto k = eval_kernel<32>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(eval)");

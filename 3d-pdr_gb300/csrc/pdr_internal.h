@@ -24,23 +24,27 @@ enum RateKind {
 
 constexpr int kWarp = 32;
 
-// Device tables of one network for the warp-per-cell integrator (neq <= 32).
+// Device tables of one network for a group of `lanes` threads integrating one
+// cell: the warp-per-cell integrator (lanes = 32, neq <= 32) and the
+// CTA-per-cell integrator (lanes = 32*ceil(neq/32), at least 64; neq <= 252
+// so that a slot fits the 8-bit field of the packed term tables).
 // Slot convention: 0..neq-1 species, neq = electron (x_e), neq+1 = constant 1.
 struct WarpTables {
   int neq = 0, nreac = 0;
+  int lanes = 0;       // table stride: threads of the group
   int rhs_len = 0;     // RHS terms per lane (balanced chunks)
   int nparts = 0;      // partial-sum slots (slot nparts is a constant zero)
   int plist_len = 0;   // partial slots summed per species
   int jac_len = 0;     // Jacobian terms per species (padded)
   int2 *rab = nullptr;        // [nreac] reactant slots (a, b)
   double *nh_mask = nullptr;  // [nreac] 1 if the rate constant is multiplied by n_H
-  int *rhs_rf = nullptr;      // [rhs_len][32] reaction | (partial slot written after the term + 1) << 16
-  double *rhs_nu = nullptr;   // [rhs_len][32] stoichiometric coefficient (0 = padding)
-  int *plist = nullptr;       // [plist_len][32] partial slots of species `lane`
-  int *jac_rab = nullptr;     // [jac_len][32] reaction | slot a << 16 | slot b << 24
-  double *jac_nu = nullptr;   // [jac_len][32]
-  float *jac_nu_f = nullptr;  // [jac_len][32]
-  double *xe_coef = nullptr;  // [32] electron-sum coefficient per slot
+  int *rhs_rf = nullptr;      // [rhs_len][lanes] reaction | (partial slot written after the term + 1) << 16
+  double *rhs_nu = nullptr;   // [rhs_len][lanes] stoichiometric coefficient (0 = padding)
+  int *plist = nullptr;       // [plist_len][lanes] partial slots of species `lane`
+  int *jac_rab = nullptr;     // [jac_len][lanes] reaction | slot a << 16 | slot b << 24
+  double *jac_nu = nullptr;   // [jac_len][lanes]
+  float *jac_nu_f = nullptr;  // [jac_len][lanes]
+  double *xe_coef = nullptr;  // [lanes] electron-sum coefficient per slot
 };
 
 // Device tables for the rate evaluator.
@@ -108,8 +112,9 @@ struct pdr_coolant {
 struct pdr_net {
   pdr::HostNet host;
   int device = -1;
-  bool warp_ok = false;
-  pdr::WarpTables warp;
+  bool warp_ok = false, cta_ok = false;
+  pdr::WarpTables warp;   // warp-per-cell tables (neq <= 32)
+  pdr::WarpTables cta;    // CTA-per-cell tables (neq <= 252)
   pdr::RateTables rates;
   std::vector<void *> allocations;
 };

@@ -234,65 +234,80 @@ int build_device_tables(pdr_net *net) {
     nhm[r] = (h.ode_kind[r] == ODE_BI || h.ode_kind[r] == ODE_GRAINH2) ? 1.0 : 0.0;
   }
   auto terms = stoichiometry(h);
-  if (neq <= kWarp) {
-    WarpTables &w = net->warp;
+  // the packed term tables hold a reaction in 16 bits and a slot in 8: larger
+  // networks get no integrator tables (the solve entry points reject them)
+  if (h.nreac >= 65536 || neq + 2 > 255) return rc;
+  auto build = [&](int G, WarpTables &w) -> int {
     w.neq = neq;
     w.nreac = h.nreac;
+    w.lanes = G;
     const int T = (int)terms.size();
-    w.rhs_len = std::max(1, (T + kWarp - 1) / kWarp);
-    if (h.nreac >= 65536 || neq + 2 > 255) return PDR_E_NET;
-    std::vector<int> rr(w.rhs_len * kWarp, 0), fl(w.rhs_len * kWarp, -1);
-    std::vector<double> nu(w.rhs_len * kWarp, 0.0);
-    std::vector<std::vector<int>> parts(kWarp);
+    // RHS: the sorted term list cut into G balanced chunks; a chunk flushes
+    // its running sum into a partial slot whenever the species changes
+    w.rhs_len = std::max(1, (T + G - 1) / G);
+    std::vector<int> rf(w.rhs_len * G, 0);
+    std::vector<double> nu(w.rhs_len * G, 0.0);
+    std::vector<std::vector<int>> parts(G);
     int slot = 0;
-    for (int l = 0; l < kWarp; l++) {
+    for (int l = 0; l < G; l++) {
       int b = l * w.rhs_len, e = std::min(T, b + w.rhs_len);
       for (int t = b; t < e; t++) {
-        int k = t - b;
-        rr[k * kWarp + l] = terms[t].r;
-        nu[k * kWarp + l] = terms[t].nu;
+        int k = t - b, fl = -1;
         if (t + 1 == e || terms[t + 1].i != terms[t].i) {
-          fl[k * kWarp + l] = slot;
+          fl = slot;
           parts[terms[t].i].push_back(slot);
           slot++;
         }
+        rf[k * G + l] = terms[t].r | ((fl + 1) << 16);
+        nu[k * G + l] = terms[t].nu;
       }
     }
+    if (slot + 1 >= 65536) return PDR_E_NET;
     w.nparts = slot;
     w.plist_len = 1;
     for (auto &p : parts) w.plist_len = std::max<int>(w.plist_len, (int)p.size());
-    std::vector<int> pl(w.plist_len * kWarp, slot /* zero slot */);
-    for (int i = 0; i < kWarp; i++)
-      for (size_t k = 0; k < parts[i].size(); k++) pl[k * kWarp + i] = parts[i][k];
+    std::vector<int> pl(w.plist_len * G, slot /* zero slot */);
+    for (int i = 0; i < G; i++)
+      for (size_t k = 0; k < parts[i].size(); k++) pl[k * G + i] = parts[i][k];
     // per-species Jacobian term lists
-    std::vector<std::vector<Term>> per(kWarp);
+    std::vector<std::vector<Term>> per(G);
     for (auto &t : terms) per[t.i].push_back(t);
     w.jac_len = 1;
     for (auto &p : per) w.jac_len = std::max<int>(w.jac_len, (int)p.size());
-    std::vector<int> jr(w.jac_len * kWarp, 0);   // reaction | a << 16 | b << 24
-    std::vector<double> jn(w.jac_len * kWarp, 0.0);
-    std::vector<float> jnf(w.jac_len * kWarp, 0.0f);
-    for (int i = 0; i < kWarp; i++)
+    std::vector<int> jr(w.jac_len * G, 0);   // reaction | a << 16 | b << 24
+    std::vector<double> jn(w.jac_len * G, 0.0);
+    std::vector<float> jnf(w.jac_len * G, 0.0f);
+    for (int i = 0; i < G; i++)
       for (size_t k = 0; k < per[i].size(); k++) {
         const int r = per[i][k].r;
-        jr[k * kWarp + i] = r | (rab[r].x << 16) | (rab[r].y << 24);
-        jn[k * kWarp + i] = per[i][k].nu;
-        jnf[k * kWarp + i] = (float)per[i][k].nu;
+        jr[k * G + i] = r | (rab[r].x << 16) | (rab[r].y << 24);
+        jn[k * G + i] = per[i][k].nu;
+        jnf[k * G + i] = (float)per[i][k].nu;
       }
-    std::vector<double> xe(kWarp, 0.0);
+    std::vector<double> xe(G, 0.0);
     for (int i = 0; i < neq; i++) xe[i] = h.xe[i];
-    w.rab = upload(net, rab, rc);
-    w.nh_mask = upload(net, nhm, rc);
-    std::vector<int> rf(rr.size());
-    for (size_t k = 0; k < rr.size(); k++) rf[k] = rr[k] | ((fl[k] + 1) << 16);
-    w.rhs_rf = upload(net, rf, rc);
-    w.rhs_nu = upload(net, nu, rc);
-    w.plist = upload(net, pl, rc);
-    w.jac_rab = upload(net, jr, rc);
-    w.jac_nu = upload(net, jn, rc);
-    w.jac_nu_f = upload(net, jnf, rc);
-    w.xe_coef = upload(net, xe, rc);
-    net->warp_ok = (rc == 0);
+    int rc2 = 0;
+    w.rab = upload(net, rab, rc2);
+    w.nh_mask = upload(net, nhm, rc2);
+    w.rhs_rf = upload(net, rf, rc2);
+    w.rhs_nu = upload(net, nu, rc2);
+    w.plist = upload(net, pl, rc2);
+    w.jac_rab = upload(net, jr, rc2);
+    w.jac_nu = upload(net, jn, rc2);
+    w.jac_nu_f = upload(net, jnf, rc2);
+    w.xe_coef = upload(net, xe, rc2);
+    return rc2;
+  };
+  if (neq <= kWarp) {
+    const int e = build(kWarp, net->warp);
+    if (e) rc = e;
+    net->warp_ok = (e == 0);
+  }
+  {
+    const int G = std::max(64, (neq + kWarp - 1) / kWarp * kWarp);
+    const int e = build(G, net->cta);
+    if (e) rc = e;
+    net->cta_ok = (e == 0);
   }
   return rc;
 }

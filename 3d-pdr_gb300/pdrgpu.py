@@ -25,7 +25,7 @@ class ChemOpts(C.Structure):
     _fields_ = [("reltol", C.c_double), ("abstol", C.c_double), ("start_time_yr", C.c_double),
                 ("end_time_yr", C.c_double), ("mxstep", C.c_long), ("precision", C.c_int),
                 ("warps_per_block", C.c_int), ("blocks_per_sm", C.c_int), ("reg_variant", C.c_int),
-                ("refill", C.c_int)]
+                ("refill", C.c_int), ("integrator", C.c_int)]
 
 
 class Phys(C.Structure):
@@ -137,13 +137,16 @@ class Network:
 
 
 def chem_opts(precision="fp64", reltol=1e-8, abstol=1e-30, start_time_yr=0.0, end_time_yr=1e7,
-              mxstep=10_000_000, warps_per_block=0, blocks_per_sm=0):
+              mxstep=10_000_000, warps_per_block=0, blocks_per_sm=0, integrator="auto"):
+    """integrator: "auto" (warp per cell for 32 ODE species, else block per
+    cell), "warp" or "block"."""
     o = ChemOpts()
     lib().pdr_chem_opts_default(C.byref(o))
     o.reltol, o.abstol, o.start_time_yr, o.end_time_yr = reltol, abstol, start_time_yr, end_time_yr
     o.mxstep = mxstep
     o.precision = PDR_MIXED if precision == "mixed" else PDR_FP64
     o.warps_per_block, o.blocks_per_sm = warps_per_block, blocks_per_sm
+    o.integrator = {"auto": 0, "warp": 1, "block": 2}[integrator]
     return o
 
 

@@ -43,6 +43,7 @@ def parse():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--ncell", type=int, default=262144)
     p.add_argument("--no-extras", action="store_true", help="headline only (profiling runs)")
+    p.add_argument("--no-autotune", action="store_true", help="default launch shape (profiling runs)")
     return p.parse_args()
 
 
@@ -169,7 +170,8 @@ def main():
     assert int(rst.abs().sum()) == 0
 
     # launch shape picked by the library's autotuner on a sample of this grid
-    opts = {p: G.autotune(net, ab0, rate, dens, G.chem_opts(p), ncell_sample=min(ncell, 8192), stream=stream)
+    opts = {p: (G.chem_opts(p) if a.no_autotune else
+                G.autotune(net, ab0, rate, dens, G.chem_opts(p), ncell_sample=min(ncell, 8192), stream=stream))
             for p in ("mixed", "fp64")}
 
     def step(precision):

@@ -54,10 +54,14 @@ typedef struct {
   double end_time_yr;   /* end_time (params.dat), used when d_t_end_yr is NULL       */
   long mxstep;          /* max internal steps per output interval (1e7, calculate_abundances.c:111) */
   int precision;        /* PDR_FP64 or PDR_MIXED                                      */
-  int warps_per_block;  /* warps (cells in flight) per block, 1..8; 0: default 4      */
+  int warps_per_block;  /* warp integrator: warps (cells in flight) per block, 1..8; 0: 4 */
   int blocks_per_sm;    /* 0: as many as fit                                          */
-  int reg_variant;      /* 0: up to ~160 registers/thread, 1: 128 (more warps per SM) */
-  int refill;           /* 0: warps refill from an atomic work queue, 1: static split */
+  int reg_variant;      /* warp integrator: 0 registers as needed (Nordsieck rows in
+                           registers), 1 at most 128 per thread (more warps per SM,
+                           Nordsieck rows in shared memory)                          */
+  int refill;           /* 0: cells refill from an atomic work queue, 1: static split */
+  int integrator;       /* 0: automatic (one warp per cell for 32 ODE species, else
+                           one block per cell), 1: warp per cell, 2: block per cell */
 } pdr_chem_opts;
 
 void pdr_chem_opts_default(pdr_chem_opts *opts);
