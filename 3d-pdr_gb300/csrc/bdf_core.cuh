@@ -32,6 +32,10 @@ constexpr double ETAMX1 = 10000.0, ETAMX2 = 10.0, ETAMX3 = 10.0, ETAMXF = 0.2, E
 constexpr double ETACF = 0.25, ADDON = 1e-6, BIAS1 = 6.0, BIAS2 = 6.0, BIAS3 = 10.0, THRESH = 1.5;
 constexpr double YEAR = 3.1556926e7;
 constexpr int FELL_BACK = 1;   // internal status: redo this cell in FP64
+// mixed form: a Newton failure with a fresh FP32 matrix is first handled as a
+// convergence failure (step size x 0.25, as CVODE does); the third such
+// failure within one step sends the cell to the FP64 pass
+constexpr int MIXED_RETRIES = 3;
 
 // shared memory of one integrator: arrays every thread reads
 struct CoefShared {
@@ -388,7 +392,7 @@ struct Core {
       predict();
       set_coeffs();
       const int r = nls(prev_fail, fallback_on_fail);
-      if (r == 2) return FELL_BACK;
+      if (r == 2 && ncf + 1 >= MIXED_RETRIES) return FELL_BACK;
       if (r != 0) {
         ncfn++;
         restore(saved_t);

@@ -46,6 +46,8 @@ int launch_chem_eval(const pdr_net *net, int nstate, const double *x, const doub
 int upload_shield_tables(int dev);
 int build_coolant_tables(pdr_coolant *c);
 int launch_levpop(const pdr_coolant *c, const LevArgsHost &h, bool mixed, int sm_count, cudaStream_t st);
+int launch_lte(const pdr_coolant *c, int ncell, const double *T, const double *density, double *pop, int *status,
+               int sm_count, cudaStream_t st);
 int launch_heating(const pdr_net *net, int network, const pdr_phys &ph, int ncell, const double *dens,
                    const double *Tg, const double *Td, const double *uv, const double *ab, const double *rate,
                    double *out, cudaStream_t st);
@@ -298,11 +300,13 @@ int pdr_chem_autotune(const pdr_net *net, int ncell_sample, const double *d_abun
   cudaEventCreate(&t0);
   cudaEventCreate(&t1);
   struct Cand { int wpb, reg, refill; };
-  const Cand warp_cands[] = {{4, 0, 0}, {2, 0, 0}, {8, 0, 0}, {4, 1, 0}, {8, 1, 0}, {4, 0, 1}};
+  const Cand warp_cands[] = {{4, 0, 0}, {2, 0, 0}, {4, 1, 0}, {8, 1, 0}, {4, 2, 0}, {2, 2, 0},
+                             {4, 3, 0}, {4, 1, 1}};
   const Cand cta_cands[] = {{0, 0, 0}, {0, 0, 1}};   // block integrator: work queue or static refill
   const bool warp_path = (opts->integrator == 1) || (opts->integrator == 0 && net->warp_ok && net->host.neq == 32);
   const Cand *cands = warp_path ? warp_cands : cta_cands;
-  const int ncand = warp_path ? 6 : 2;
+  const int ncand = warp_path ? 8 : 2;
+  const bool log = getenv("PDR_AUTOTUNE_LOG") != nullptr;
   float best = 1e30f;
   pdr_chem_opts best_o = *opts;
   int rc = 0;
@@ -323,6 +327,9 @@ int pdr_chem_autotune(const pdr_net *net, int ncell_sample, const double *d_abun
     if (e != cudaSuccess) { rc = cuda_fail(e, "autotune run"); break; }
     float ms = 0.f;
     cudaEventElapsedTime(&ms, t0, t1);
+    if (log)
+      fprintf(stderr, "pdr_chem_autotune: warps_per_block %d reg_variant %d refill %d: %.3f ms\n", c.wpb, c.reg,
+              c.refill, ms);
     if (ms < best) { best = ms; best_o = o; }
   }
   cudaEventDestroy(t0);
@@ -414,6 +421,19 @@ int pdr_levpop_batched(const pdr_coolant *c, int ncell, int nrays, const double 
   h.density = d_density; h.T = d_T; h.Td = d_Tdust; h.partner5 = d_partner5; h.cdens = d_coolant_density;
   h.spop = d_spop; h.tau = d_tau; h.pop = d_pop; h.cooling = d_cooling; h.line = d_line; h.status = d_status;
   return launch_levpop(c, h, precision == PDR_MIXED, sms, (cudaStream_t)stream);
+}
+
+int pdr_lte_batched(const pdr_coolant *c, int ncell, const double *d_T, const double *d_density, double *d_pop,
+                    int *d_status, void *stream) {
+  if (!c || ncell < 0 || !d_T || !d_density || !d_pop) {
+    set_error("pdr_lte_batched: invalid argument");
+    return PDR_E_ARG;
+  }
+  if (ncell == 0) return 0;
+  int dev = 0, sms = 0;
+  int rc = current_device(&dev, &sms);
+  if (rc) return rc;
+  return launch_lte(c, ncell, d_T, d_density, d_pop, d_status, sms, (cudaStream_t)stream);
 }
 
 int pdr_heating_batched(const pdr_net *net, int network, const pdr_phys *phys, int ncell, const double *d_density,

@@ -18,7 +18,10 @@
 //        unpivoted row of largest magnitude, lowest row on ties), rows kept in
 //        place with the pivot order recorded; right-looking in panels of 8
 //        columns: per panel the pivot rows' U block is formed column-parallel
-//        and the trailing update is a rank-8 update applied by the row owners;
+//        and the trailing update is a rank-8 update applied by the row owners
+//        to the columns where that U block has a nonzero (the network's
+//        Jacobian is sparse, so many are exactly zero -- skipping them changes
+//        no result);
 //   solve forward/backward substitution in 32-row blocks: the 32x32 diagonal
 //        blocks of L and U are inverted in place at setup, so a block step is
 //        a 32x32 product by one warp plus a rank-32 update by the row owners.
@@ -71,7 +74,7 @@ struct CtaArgs {
 
 // byte offsets of the block's shared arrays (host and device agree)
 struct CtaLayout {
-  size_t scr, xs, part, red, sig, perm, bsv, ys, upan, ws, mat, total;
+  size_t scr, xs, part, red, sig, perm, cols, bsv, ys, upan, ws, mat, total;
 };
 
 __host__ __device__ inline size_t al16(size_t x) { return (x + 15) & ~size_t(15); }
@@ -87,6 +90,7 @@ __host__ __device__ inline CtaLayout cta_layout(int n, int nreac, int nparts, in
   L.red = o; o += al16(2 * MAXW * (8 + 8 + 4));   // sums, argmax keys, argmax rows
   L.sig = o; o += al16(4 * (size_t)(n + 2));
   L.perm = o; o += al16(4 * (size_t)n);
+  L.cols = o; o += al16(4 * (size_t)(n + MAXW));   // nonzero U columns of a panel, per-warp counts
   L.bsv = o; o += al16(mt * (size_t)G);
   L.ys = o; o += al16(mt * (size_t)(n + DB));
   L.upan = o; o += al16(mt * PB * (size_t)n);
@@ -130,6 +134,7 @@ struct CtaCell : Core<CtaCell<MIXED>> {
   int *red_i;            // [2][MAXW] argmax rows
   float *sig;
   int *perm;
+  int *cols, *cnt;       // nonzero columns of the current U panel; per-warp counts
   MT *bsv, *ys, *upan, *mat;
   int rbuf = 0;          // alternating reduction buffer
   double cx;
@@ -196,6 +201,7 @@ struct CtaCell : Core<CtaCell<MIXED>> {
     if (owns) xs[tid] = yv;
     const double xe = sum_all(owns ? cx * yv : 0.0);
     this->xe_last = xe;
+#pragma unroll 4
     for (int r = tid; r < T.nreac; r += G) {
       const int2 ab = __ldg(&T.rab[r]);
       scr[r] = kn[r] * slot_value(ab.x, xe) * slot_value(ab.y, xe);
@@ -212,6 +218,7 @@ struct CtaCell : Core<CtaCell<MIXED>> {
     }
     __syncthreads();
     double f = 0.0;
+#pragma unroll 4
     for (int k = 0; k < T.plist_len; k++) f += part[__ldg(&T.plist[k * G + tid])];
     this->nfe++;
     return owns ? f : 0.0;
@@ -230,6 +237,7 @@ struct CtaCell : Core<CtaCell<MIXED>> {
     const double xe = sum_all(owns ? cx * yv : 0.0);
     MT *Da = reinterpret_cast<MT *>(scr);
     MT *Db = Da + T.nreac;
+#pragma unroll 4
     for (int r = tid; r < T.nreac; r += G) {
       const int2 ab = __ldg(&T.rab[r]);
       const double k = kn[r];
@@ -245,6 +253,8 @@ struct CtaCell : Core<CtaCell<MIXED>> {
       for (int j = 0; j < n + 2; j++) M(tid, j) = MT(0);
     __syncthreads();
     if (owns) {
+      // the term tables are read from L2: keep several loads in flight
+#pragma unroll 8
       for (int t = 0; t < T.jac_len; t++) {
         MT nu;
         if constexpr (MIXED) nu = __ldg(&T.jac_nu_f[t * G + tid]);
@@ -293,8 +303,12 @@ struct CtaCell : Core<CtaCell<MIXED>> {
         }
       }
       __syncthreads();
-      // U rows of this panel's pivots, columns right of the panel
-      for (int j = k0 + kb + tid; j < n; j += blockDim.x) {
+      // U rows of this panel's pivots, columns right of the panel (at most one
+      // column per thread: the block has at least n threads); the columns
+      // whose U entries are all zero are left out of the trailing update
+      const int j = k0 + kb + tid;
+      bool nzc = false;
+      if (j < n) {
         MT u[PB];
 #pragma unroll
         for (int t = 0; t < PB; t++) {
@@ -306,22 +320,41 @@ struct CtaCell : Core<CtaCell<MIXED>> {
               if (t2 < t) s = fma(-M(pt, k0 + t2), u[t2], s);
             u[t] = s;
             M(pt, j) = s;
+            nzc |= (s != MT(0));
           } else {
             u[t] = MT(0);
           }
           upan[(size_t)j * PB + t] = u[t];
         }
       }
+      const unsigned bal = __ballot_sync(FULL, nzc);
+      if (lane == 0) cnt[warp] = __popc(bal);
+      __syncthreads();
+      int base = 0, ncols = 0;
+      for (int w = 0; w < nw; w++) {
+        const int c = cnt[w];
+        base += (w < warp) ? c : 0;
+        ncols += c;
+      }
+      if (nzc) cols[base + __popc(bal & ((1u << lane) - 1u))] = j;
       __syncthreads();
       if (mystep < 0) {
         MT l[PB];
+        bool any = false;
 #pragma unroll
-        for (int t = 0; t < PB; t++) l[t] = (t < kb) ? M(tid, k0 + t) : MT(0);
-        for (int j = k0 + kb; j < n; j++) {
-          MT s = M(tid, j);
+        for (int t = 0; t < PB; t++) {
+          l[t] = (t < kb) ? M(tid, k0 + t) : MT(0);
+          any |= (l[t] != MT(0));
+        }
+        if (any) {
+#pragma unroll 4
+          for (int c = 0; c < ncols; c++) {
+            const int jj = cols[c];
+            MT s = M(tid, jj);
 #pragma unroll
-          for (int t = 0; t < PB; t++) s = fma(-l[t], upan[(size_t)j * PB + t], s);
-          M(tid, j) = s;
+            for (int t = 0; t < PB; t++) s = fma(-l[t], upan[(size_t)jj * PB + t], s);
+            M(tid, jj) = s;
+          }
         }
       }
     }
@@ -523,6 +556,8 @@ __global__ void __launch_bounds__(256, 1) chem_cta_kernel(const __grid_constant_
   c.red_i = reinterpret_cast<int *>(smem_raw + L.red + 2 * MAXW * 16);
   c.sig = reinterpret_cast<float *>(smem_raw + L.sig);
   c.perm = reinterpret_cast<int *>(smem_raw + L.perm);
+  c.cols = reinterpret_cast<int *>(smem_raw + L.cols);
+  c.cnt = c.cols + A.n;
   c.bsv = reinterpret_cast<MT *>(smem_raw + L.bsv);
   c.ys = reinterpret_cast<MT *>(smem_raw + L.ys);
   c.upan = reinterpret_cast<MT *>(smem_raw + L.upan);
@@ -577,12 +612,26 @@ size_t chem_cta_global_bytes(const pdr_net *net, bool mixed, int grid) {
   return b;
 }
 
+// The dynamic shared-memory limit of a kernel only ever grows (networks of
+// different sizes share the two kernels), so no call lowers it below what
+// another network's launch needs.
+static cudaError_t ensure_smem_attr(bool mixed, size_t smem) {
+  static std::mutex mu;
+  static size_t attr[2] = {0, 0};
+  std::lock_guard<std::mutex> lk(mu);
+  if (smem <= attr[mixed]) return cudaSuccess;
+  auto k = mixed ? chem_cta_kernel<true> : chem_cta_kernel<false>;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess) attr[mixed] = smem;
+  return e;
+}
+
 // blocks per SM the block integrator runs with (0 on error)
 int chem_cta_blocks_per_sm(const pdr_net *net, bool mixed) {
   bool ms = false;
   const size_t smem = chem_cta_smem(net, mixed, &ms);
   auto k = mixed ? chem_cta_kernel<true> : chem_cta_kernel<false>;
-  if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
+  if (ensure_smem_attr(mixed, smem) != cudaSuccess) return 0;
   int per_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, net->cta.lanes, smem) != cudaSuccess) return 0;
   return per_sm;
@@ -626,16 +675,8 @@ int launch_chem_cta(const pdr_net *net, int ncell, double *ab, const double *rat
   A.kn_global = reinterpret_cast<double *>(scratch);
   A.mat_global = ms ? nullptr : reinterpret_cast<unsigned char *>(scratch) + al16((size_t)grid * T.nreac * 8);
   auto k = mixed ? chem_cta_kernel<true> : chem_cta_kernel<false>;
-  static std::mutex mu;
-  static size_t cached[2] = {0, 0};
-  {
-    std::lock_guard<std::mutex> lk(mu);
-    if (cached[mixed] != smem) {
-      cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(chem_cta_kernel)");
-      cached[mixed] = smem;
-    }
-  }
+  cudaError_t ea = ensure_smem_attr(mixed, smem);
+  if (ea != cudaSuccess) return cuda_fail(ea, "cudaFuncSetAttribute(chem_cta_kernel)");
   k<<<grid, T.lanes, smem, st>>>(A, ncell, total_ptr, ms ? 1 : 0);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? 0 : cuda_fail(e, "chem_cta_kernel launch");

@@ -326,11 +326,20 @@ struct WarpCell : Core<WarpCell<NSP, MIXED, ZSH>, ZSH> {
   }
 };
 
-// MINB = 1 lets the compiler use the registers it wants (8-12 warps/SM,
-// Nordsieck rows in registers); MINB = 2 caps them at 128 for 16 warps/SM
-// and keeps the Nordsieck rows in shared memory; the autotuner picks.
-template <int NSP, bool MIXED, int MINB>
-__global__ void __launch_bounds__(256, MINB) chem_warp_kernel(const __grid_constant__ ChemArgs A, int total_cells, const int *total_ptr) {
+// Register variants (the autotuner picks): RV 0 lets the compiler use the
+// registers it wants (about 230; 8 warps/SM); RV 1 caps them at 128 for 16
+// warps/SM with the Nordsieck rows in shared memory; RV 2 and 3 cap them at
+// 168 for 12 warps/SM (blocks of at most 4 warps), Nordsieck rows in
+// registers (2) or shared memory (3).
+template <int RV> struct RegVariant;
+template <> struct RegVariant<0> { static constexpr int threads = 256, min_blocks = 1; static constexpr bool zsh = false; };
+template <> struct RegVariant<1> { static constexpr int threads = 256, min_blocks = 2; static constexpr bool zsh = true; };
+template <> struct RegVariant<2> { static constexpr int threads = 128, min_blocks = 3; static constexpr bool zsh = false; };
+template <> struct RegVariant<3> { static constexpr int threads = 128, min_blocks = 3; static constexpr bool zsh = true; };
+
+template <int NSP, bool MIXED, int RV>
+__global__ void __launch_bounds__(RegVariant<RV>::threads, RegVariant<RV>::min_blocks)
+    chem_warp_kernel(const __grid_constant__ ChemArgs A, int total_cells, const int *total_ptr) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   using MT = typename std::conditional<MIXED, float, double>::type;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -338,7 +347,7 @@ __global__ void __launch_bounds__(256, MINB) chem_warp_kernel(const __grid_const
   // per-warp shared layout
   const size_t kn_b = (size_t)nreac * 8, scr_b = (size_t)nreac * 16, xs_b = 8 * (NSP + 2);
   const size_t part_b = 8 * (A.tab.nparts + 1);
-  constexpr bool ZSH = (MINB >= 2);
+  constexpr bool ZSH = RegVariant<RV>::zsh;
   const size_t jrow_b = sizeof(MT) * NSP * (NSP + 3), sig_b = 4 * (NSP + 2) + 4 * NSP;
   const size_t ws_b = sizeof(CoefShared) + (ZSH ? 8 * (QMAX + 1) * kWarp : 0);
   auto al = [](size_t x) { return (x + 15) & ~size_t(15); };
@@ -464,23 +473,35 @@ int launch_chem_warp(const pdr_net *net, int ncell, double *ab, const double *ra
   A.refill_static = (o.refill == 1) ? 1 : 0;
   const int wpb = o.warps_per_block > 0 ? o.warps_per_block : 4;
   if (wpb > 8) return PDR_E_ARG;
-  const size_t smem = chem_warp_smem_per_warp(32, A.nreac, T.nparts, mixed, o.reg_variant == 1) * wpb;
-  const int variant = (mixed ? 2 : 0) + (o.reg_variant == 1 ? 1 : 0);
+  const int rv = (o.reg_variant >= 0 && o.reg_variant <= 3) ? o.reg_variant : 0;
+  if (rv >= 2 && wpb > 4) return PDR_E_ARG;   // those variants launch at most 128 threads per block
+  const bool zsh = (rv == 1 || rv == 3);
+  const size_t smem = chem_warp_smem_per_warp(32, A.nreac, T.nparts, mixed, zsh) * wpb;
+  const int variant = (mixed ? 4 : 0) + rv;
   using KFn = void (*)(ChemArgs, int, const int *);
-  static const KFn kernels[4] = {chem_warp_kernel<32, false, 1>, chem_warp_kernel<32, false, 2>,
-                                 chem_warp_kernel<32, true, 1>, chem_warp_kernel<32, true, 2>};
-  // attribute and occupancy per (variant, block size, smem), cached so that
-  // calls made while a stream is being captured issue no attribute changes
+  static const KFn kernels[8] = {chem_warp_kernel<32, false, 0>, chem_warp_kernel<32, false, 1>,
+                                 chem_warp_kernel<32, false, 2>, chem_warp_kernel<32, false, 3>,
+                                 chem_warp_kernel<32, true, 0>,  chem_warp_kernel<32, true, 1>,
+                                 chem_warp_kernel<32, true, 2>,  chem_warp_kernel<32, true, 3>};
+  // The dynamic shared-memory limit is an attribute of the function: it only
+  // ever grows (to the largest block size used so far), so that a launch with
+  // fewer warps never lowers it below what another block size needs.  The
+  // occupancy is cached per (variant, block size); calls made while a stream
+  // is being captured then issue no attribute changes.
   static std::mutex mu;
-  static int cached_per_sm[4][9] = {};
-  static size_t cached_smem[4][9] = {};
+  static size_t attr_smem[8] = {};
+  static int cached_per_sm[8][9] = {};
+  static size_t cached_smem[8][9] = {};
   int per_sm = 0;
   cudaError_t e = cudaSuccess;
   {
     std::lock_guard<std::mutex> lk(mu);
-    if (cached_smem[variant][wpb] != smem) {
+    if (smem > attr_smem[variant]) {
       e = cudaFuncSetAttribute(kernels[variant], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute");
+      attr_smem[variant] = smem;
+    }
+    if (cached_smem[variant][wpb] != smem) {
       e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&cached_per_sm[variant][wpb], kernels[variant], wpb * 32, smem);
       if (e != cudaSuccess) return cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
       cached_smem[variant][wpb] = smem;

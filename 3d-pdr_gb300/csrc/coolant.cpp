@@ -161,6 +161,7 @@ int build_coolant_tables(pdr_coolant *c) {
   t.B = up(c, h.B, rc);
   t.freq = up(c, h.freq, rc);
   t.weights = up(c, h.weights, rc);
+  t.energies = up(c, h.energies, rc);
   t.line_of_pair = up(c, lop, rc);
   return rc;
 }

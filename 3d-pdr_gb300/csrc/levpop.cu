@@ -17,6 +17,8 @@
 //   iterative-refinement step, verified by the size of the next correction
 //   (cells that fail the check are re-solved in FP64, status 2); negative
 //   populations are set to zero.
+#include <algorithm>
+
 #include "pdr_internal.h"
 
 namespace pdr {
@@ -329,6 +331,36 @@ __global__ void __launch_bounds__(256) levpop_kernel(const __grid_constant__ Coo
 }  // namespace
 
 size_t levpop_smem_per_warp(int n) { return levpop_warp_bytes(n); }
+
+namespace {
+// LTE populations of one cell per thread: CALCULATE_PARTITION_FUNCTION and
+// CALCULATE_LTE_POPULATIONS (3DPDR.F90:1847-1894), the same operation order;
+// the reference STOPs when the populations do not add up to the density
+// within 1e-3 -- here the cell's status is set to 1 instead.
+__global__ void lte_kernel(CoolantTables C, int ncell, const double *__restrict__ T,
+                           const double *__restrict__ density, double *__restrict__ pop, int *status) {
+  for (int cell = blockIdx.x * blockDim.x + threadIdx.x; cell < ncell; cell += gridDim.x * blockDim.x) {
+    const double t = T[cell], d = density[cell];
+    double z = 0.0;
+    for (int i = 0; i < C.nlev; i++) z = z + C.weights[i] * exp(-C.energies[i] / KB / t);
+    double tot = 0.0;
+    for (int i = 0; i < C.nlev; i++) {
+      const double p = d * C.weights[i] * exp(-C.energies[i] / KB / t) / z;
+      pop[(size_t)cell * C.nlev + i] = p;
+      tot = tot + p;
+    }
+    if (status) status[cell] = (fabs(tot - d) / d > 1.0e-3) ? 1 : 0;
+  }
+}
+}  // namespace
+
+int launch_lte(const pdr_coolant *c, int ncell, const double *T, const double *density, double *pop, int *status,
+               int sm_count, cudaStream_t st) {
+  const int blocks = std::min((ncell + 127) / 128, sm_count * 8);
+  lte_kernel<<<blocks, 128, 0, st>>>(c->dev, ncell, T, density, pop, status);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? 0 : cuda_fail(e, "lte_kernel launch");
+}
 
 int launch_levpop(const pdr_coolant *c, const LevArgsHost &h, bool mixed, int sm_count, cudaStream_t st) {
   LevArgs A;

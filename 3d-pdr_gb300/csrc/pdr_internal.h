@@ -88,6 +88,7 @@ struct CoolantTables {
   double *temps = nullptr;     // [npart][ntemp]
   double *col = nullptr;       // [npart][ntemp][nlev*nlev]
   double *A = nullptr, *B = nullptr, *freq = nullptr, *weights = nullptr;
+  double *energies = nullptr;  // [nlev] level energies, erg
   int *line_of_pair = nullptr; // [nlev*nlev] radiative line of (i,j), i>j, else -1
 };
 

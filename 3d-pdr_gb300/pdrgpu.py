@@ -76,6 +76,7 @@ def lib():
     L.pdr_coolant_info.argtypes = [_vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]
     L.pdr_levpop_batched.argtypes = [_vp, C.c_int, C.c_int] + [_vp] * 7 + [C.c_int, C.c_double, C.c_double,
                                                                           C.c_int] + [_vp] * 5
+    L.pdr_lte_batched.argtypes = [_vp, C.c_int] + [_vp] * 5
     _LIB = L
     return L
 
@@ -277,6 +278,17 @@ def level_populations(cool, density, T, Tdust, partner5, coolant_density, spop, 
                                    PDR_MIXED if precision == "mixed" else PDR_FP64, _ptr(pop), _ptr(cooling),
                                    _ptr(line), _ptr(status), _stream(stream)), "pdr_levpop_batched")
     return pop, cooling, line, status
+
+
+def lte_populations(cool, T, density, stream=None):
+    """LTE level populations (ncell, nlev) and the per-cell status."""
+    import torch
+    ncell = T.shape[0]
+    pop = torch.empty((ncell, cool.nlev), dtype=torch.float64, device=T.device)
+    status = torch.empty(ncell, dtype=torch.int32, device=T.device)
+    check(lib().pdr_lte_batched(cool.handle, ncell, _ptr(T), _ptr(density), _ptr(pop), _ptr(status),
+                                _stream(stream)), "pdr_lte_batched")
+    return pop, status
 
 
 def heating(net, network, ph, density, Tgas, Tdust, uv_field, abundance, rate, stream=None):

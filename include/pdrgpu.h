@@ -56,9 +56,11 @@ typedef struct {
   int precision;        /* PDR_FP64 or PDR_MIXED                                      */
   int warps_per_block;  /* warp integrator: warps (cells in flight) per block, 1..8; 0: 4 */
   int blocks_per_sm;    /* 0: as many as fit                                          */
-  int reg_variant;      /* warp integrator: 0 registers as needed (Nordsieck rows in
-                           registers), 1 at most 128 per thread (more warps per SM,
-                           Nordsieck rows in shared memory)                          */
+  int reg_variant;      /* warp integrator register budget: 0 as needed (8 warps/SM),
+                           1 at most 128 per thread (16 warps/SM, Nordsieck rows in
+                           shared memory), 2 at most 168 (12 warps/SM), 3 as 2 with
+                           the Nordsieck rows in shared memory; 2 and 3 take at most
+                           4 warps per block                                          */
   int refill;           /* 0: cells refill from an atomic work queue, 1: static split */
   int integrator;       /* 0: automatic (one warp per cell for 32 ODE species, else
                            one block per cell), 1: warp per cell, 2: block per cell */
@@ -169,6 +171,13 @@ int pdr_levpop_batched(const pdr_coolant *c, int ncell, int nrays, const double 
                        const double *d_coolant_density, const double *d_spop, const double *d_tau,
                        int pseudo1d, double metallicity, double g2d, int precision, double *d_pop,
                        double *d_cooling, double *d_line, int *d_status, void *stream);
+
+/* LTE level populations (CALCULATE_PARTITION_FUNCTION + CALCULATE_LTE_POPULATIONS,
+ * 3DPDR.F90:1847-1894): d_pop[ncell*nlev] = n g_i exp(-E_i/kT) / Z for every
+ * cell; d_status[ncell] (or NULL) is 1 where the populations miss the density
+ * by more than 1e-3 (where the reference STOPs), else 0. */
+int pdr_lte_batched(const pdr_coolant *c, int ncell, const double *d_T, const double *d_density, double *d_pop,
+                    int *d_status, void *stream);
 
 /* ---- heating: batched CALC_HEATING (sub_calculate_heating.F90:7-386) ----
  * network 0 = reduced, 1 = full (the reference's compile-time choice of the

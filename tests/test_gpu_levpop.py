@@ -89,3 +89,17 @@ def test_heating_matches_oracle(cuda, name, network):
                     dev(rates, cuda)).cpu().numpy()
     scale = np.abs(ref).max(axis=1, keepdims=True)
     assert (np.abs(got - ref) / scale).max() < TOL
+
+
+@pytest.mark.parametrize("key", ["CII", "CI", "OI", "CO"])
+def test_lte_matches_oracle(cuda, key):
+    """LTE populations (3DPDR.F90:1847-1894) within 1e-13 relative."""
+    oc = O.Coolant(key)
+    lp = W.levpop(ncell=256, seed=31)
+    dens = lp["n_H"] * W.COOLANT_X[key]
+    ref = np.array([oc.lte(T, d) for T, d in zip(lp["T"], dens)])
+    pop, status = G.lte_populations(G.Coolant(key), dev(lp["T"], cuda), dev(dens, cuda))
+    pop, status = pop.cpu().numpy(), status.cpu().numpy()
+    assert (status == 0).all()
+    m = ref > 1e-300
+    assert (np.abs(pop - ref)[m] / ref[m]).max() < 1e-13
