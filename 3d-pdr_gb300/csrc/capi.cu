@@ -130,6 +130,98 @@ static int cta_per_sm(const pdr_net *net, bool mixed) {
   return v;
 }
 
+
+static bool uses_warp_path(const pdr_net *net, const pdr_chem_opts &o) {
+  return (o.integrator == 1) || (o.integrator == 0 && net->warp_ok && net->host.neq == 32);
+}
+
+static int check_opts(const pdr_net *net, const pdr_chem_opts &o, const char *who) {
+  if (!(o.reltol >= 0.0) || !(o.abstol > 0.0) || o.mxstep <= 0 ||
+      (o.precision != PDR_FP64 && o.precision != PDR_MIXED) || o.integrator < 0 || o.integrator > 2) {
+    set_error(std::string(who) + ": invalid options");
+    return PDR_E_ARG;
+  }
+  const bool warp_ok = net->warp_ok && net->host.neq == 32;
+  const bool warp_path = uses_warp_path(net, o);
+  if ((warp_path && !warp_ok) || (!warp_path && !net->cta_ok)) {
+    set_error(std::string(who) + (warp_path ? ": the warp integrator takes networks of 32 ODE species"
+                                            : ": the network is too large for the integrator tables"));
+    return PDR_E_NET;
+  }
+  return 0;
+}
+
+// SMs the persistent grid spans
+static int eff_sms(const pdr_chem_opts &o, int sms) { return (o.max_sms > 0 && o.max_sms < sms) ? o.max_sms : sms; }
+
+// grid of the block integrator for one precision
+static int cta_grid(const pdr_net *net, const pdr_chem_opts &o, bool mixed, int sms) {
+  sms = eff_sms(o, sms);
+  int per_sm = cta_per_sm(net, mixed);
+  if (per_sm < 1) per_sm = 1;
+  if (o.blocks_per_sm > 0 && o.blocks_per_sm < per_sm) per_sm = o.blocks_per_sm;
+  return sms * per_sm;
+}
+
+// bytes of block-integrator scratch one solve needs (both passes of the mixed form)
+static size_t cta_bytes_needed(const pdr_net *net, const pdr_chem_opts &o, int sms) {
+  const bool mixed = (o.precision == PDR_MIXED);
+  size_t bytes = chem_cta_global_bytes(net, mixed, cta_grid(net, o, mixed, sms));
+  if (mixed) bytes = std::max(bytes, chem_cta_global_bytes(net, false, cta_grid(net, o, false, sms)));
+  return bytes;
+}
+
+// One batched solve with the given scratch: the mixed pass (or the FP64 pass)
+// over all cells, then, for the mixed form, the FP64 pass over the cells it
+// queued.  grow = false: the scratch must already be large enough (no allocation).
+static int solve_core(const pdr_net *net, int ncell, double *ab, const double *rate, const double *dens,
+                      const double *tend, const pdr_chem_opts &o, int *status, int *stats, Scratch *s, bool grow,
+                      int sms, cudaStream_t st) {
+  if (s->redo_cap < (size_t)ncell) {
+    set_error("pdr: solver scratch holds fewer cells than the call");
+    return PDR_E_ARG;
+  }
+  cudaError_t e = cudaMemsetAsync(s->counters, 0, 4 * sizeof(int), st);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(scratch)");
+  const bool mixed = (o.precision == PDR_MIXED);
+  int rc;
+  if (uses_warp_path(net, o)) {
+    const int sm_use = eff_sms(o, sms);
+    rc = launch_chem_warp(net, ncell, ab, rate, dens, tend, o, status, stats, s->counters + 0, s->redo,
+                          s->counters + 2, nullptr, nullptr, mixed, sm_use, st);
+    if (rc || !mixed) return rc;
+    // cells whose FP32 Newton iteration failed are re-solved in FP64
+    return launch_chem_warp(net, ncell, ab, rate, dens, tend, o, status, stats, s->counters + 1, nullptr, nullptr,
+                            s->redo, s->counters + 2, false, sm_use, st);
+  }
+  // one block per cell: persistent grid of SMs x resident blocks
+  const size_t bytes = cta_bytes_needed(net, o, sms);
+  if (grow) {
+    rc = cta_scratch(s, bytes);
+    if (rc) return rc;
+  } else if (s->cta_bytes < bytes) {
+    set_error("pdr: solver scratch is too small for the block integrator");
+    return PDR_E_ARG;
+  }
+  rc = launch_chem_cta(net, ncell, ab, rate, dens, tend, o, status, stats, s->counters + 0, s->redo, s->counters + 2,
+                       nullptr, nullptr, mixed, cta_grid(net, o, mixed, sms), s->cta, st);
+  if (rc || !mixed) return rc;
+  return launch_chem_cta(net, ncell, ab, rate, dens, tend, o, status, stats, s->counters + 1, nullptr, nullptr,
+                         s->redo, s->counters + 2, false, cta_grid(net, o, false, sms), s->cta, st);
+}
+
+}  // namespace pdr
+
+// A solver instance: its own scratch, sized once, so that runs allocate
+// nothing and instances on different streams can overlap.
+struct pdr_solver {
+  const pdr_net *net = nullptr;
+  pdr_chem_opts opts;
+  int max_cells = 0, sms = 0, dev = 0;
+  pdr::Scratch s;
+};
+
+namespace pdr {
 }  // namespace pdr
 
 using namespace pdr;
@@ -148,9 +240,10 @@ void pdr_chem_opts_default(pdr_chem_opts *o) {
   o->precision = PDR_FP64;
   o->warps_per_block = 0;
   o->blocks_per_sm = 0;
-  o->reg_variant = 0;
+  o->reg_variant = 2;   // 168 registers, 12 warps per SM: the fastest variant measured on GB300
   o->refill = 0;
   o->integrator = 0;
+  o->max_sms = 0;
 }
 
 int pdr_device_info(int *sm_count, int *cc_major, int *cc_minor) {
@@ -221,65 +314,65 @@ int pdr_chem_solve_batched(const pdr_net *net, int ncell, double *d_abundance, c
   pdr_chem_opts o;
   pdr_chem_opts_default(&o);
   if (opts) o = *opts;
-  if (!(o.reltol >= 0.0) || !(o.abstol > 0.0) || o.mxstep <= 0 ||
-      (o.precision != PDR_FP64 && o.precision != PDR_MIXED)) {
-    set_error("pdr_chem_solve_batched: invalid options");
-    return PDR_E_ARG;
-  }
-  if (o.integrator < 0 || o.integrator > 2) {
-    set_error("pdr_chem_solve_batched: invalid integrator choice");
-    return PDR_E_ARG;
-  }
-  const bool warp_ok = net->warp_ok && net->host.neq == 32;
-  const bool warp_path = (o.integrator == 1) || (o.integrator == 0 && warp_ok);
-  if ((warp_path && !warp_ok) || (!warp_path && !net->cta_ok)) {
-    set_error(warp_path ? "pdr_chem_solve_batched: the warp integrator takes networks of 32 ODE species"
-                        : "pdr_chem_solve_batched: the network is too large for the integrator tables");
-    return PDR_E_NET;
-  }
+  int rc = check_opts(net, o, "pdr_chem_solve_batched");
+  if (rc) return rc;
   int dev = 0, sms = 0;
-  int rc = current_device(&dev, &sms);
+  rc = current_device(&dev, &sms);
   if (rc) return rc;
   Scratch *s = nullptr;
   rc = scratch_for(dev, (size_t)ncell, &s);
   if (rc) return rc;
-  cudaStream_t st = (cudaStream_t)stream;
-  cudaError_t e = cudaMemsetAsync(s->counters, 0, 4 * sizeof(int), st);
-  if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(scratch)");
-  const bool mixed = (o.precision == PDR_MIXED);
-  if (warp_path) {
-    rc = launch_chem_warp(net, ncell, d_abundance, d_rate, d_density, d_t_end_yr, o, d_status, d_stats,
-                          s->counters + 0, s->redo, s->counters + 2, nullptr, nullptr, mixed, sms, st);
-    if (rc) return rc;
-    if (mixed) {
-      // cells whose FP32 Newton iteration failed are re-solved in FP64
-      rc = launch_chem_warp(net, ncell, d_abundance, d_rate, d_density, d_t_end_yr, o, d_status, d_stats,
-                            s->counters + 1, nullptr, nullptr, s->redo, s->counters + 2, false, sms, st);
-      if (rc) return rc;
-    }
-    return 0;
+  return solve_core(net, ncell, d_abundance, d_rate, d_density, d_t_end_yr, o, d_status, d_stats, s, true, sms,
+                    (cudaStream_t)stream);
+}
+
+int pdr_solver_create(const pdr_net *net, int max_cells, const pdr_chem_opts *opts, pdr_solver **out) {
+  if (!net || max_cells <= 0 || !out) {
+    set_error("pdr_solver_create: invalid argument");
+    return PDR_E_ARG;
   }
-  // one block per cell: persistent grid of SMs x resident blocks
-  auto grid_of = [&](bool m) {
-    int per_sm = cta_per_sm(net, m);
-    if (per_sm < 1) per_sm = 1;
-    if (o.blocks_per_sm > 0 && o.blocks_per_sm < per_sm) per_sm = o.blocks_per_sm;
-    return sms * per_sm;
-  };
-  const int grid1 = grid_of(mixed), grid2 = mixed ? grid_of(false) : 0;
-  size_t bytes = chem_cta_global_bytes(net, mixed, grid1);
-  if (mixed) bytes = std::max(bytes, chem_cta_global_bytes(net, false, grid2));
-  rc = cta_scratch(s, bytes);
+  *out = nullptr;
+  pdr_chem_opts o;
+  pdr_chem_opts_default(&o);
+  if (opts) o = *opts;
+  int rc = check_opts(net, o, "pdr_solver_create");
   if (rc) return rc;
-  rc = launch_chem_cta(net, ncell, d_abundance, d_rate, d_density, d_t_end_yr, o, d_status, d_stats,
-                       s->counters + 0, s->redo, s->counters + 2, nullptr, nullptr, mixed, grid1, s->cta, st);
-  if (rc) return rc;
-  if (mixed) {
-    rc = launch_chem_cta(net, ncell, d_abundance, d_rate, d_density, d_t_end_yr, o, d_status, d_stats,
-                         s->counters + 1, nullptr, nullptr, s->redo, s->counters + 2, false, grid2, s->cta, st);
-    if (rc) return rc;
+  pdr_solver *v = new pdr_solver();
+  v->net = net;
+  v->opts = o;
+  v->max_cells = max_cells;
+  rc = current_device(&v->dev, &v->sms);
+  cudaError_t e = cudaSuccess;
+  if (!rc && (e = cudaMalloc(&v->s.counters, 4 * sizeof(int))) != cudaSuccess) rc = cuda_fail(e, "cudaMalloc(solver)");
+  if (!rc && (e = cudaMalloc(&v->s.redo, sizeof(int) * (size_t)max_cells)) != cudaSuccess)
+    rc = cuda_fail(e, "cudaMalloc(solver)");
+  if (!rc) v->s.redo_cap = (size_t)max_cells;
+  if (!rc && !uses_warp_path(net, o)) rc = cta_scratch(&v->s, cta_bytes_needed(net, o, v->sms));
+  if (rc) {
+    pdr_solver_free(v);
+    return rc;
   }
+  *out = v;
   return 0;
+}
+
+int pdr_solver_run(pdr_solver *v, int ncell, double *d_abundance, const double *d_rate, const double *d_density,
+                   const double *d_t_end_yr, int *d_status, int *d_stats, void *stream) {
+  if (!v || ncell < 0 || ncell > v->max_cells || !d_abundance || !d_rate || !d_density || !d_status) {
+    set_error("pdr_solver_run: invalid argument (ncell above the solver's max_cells?)");
+    return PDR_E_ARG;
+  }
+  if (ncell == 0) return 0;
+  return solve_core(v->net, ncell, d_abundance, d_rate, d_density, d_t_end_yr, v->opts, d_status, d_stats, &v->s,
+                    false, v->sms, (cudaStream_t)stream);
+}
+
+void pdr_solver_free(pdr_solver *v) {
+  if (!v) return;
+  if (v->s.counters) cudaFree(v->s.counters);
+  if (v->s.redo) cudaFree(v->s.redo);
+  if (v->s.cta) cudaFree(v->s.cta);
+  delete v;
 }
 
 int pdr_chem_autotune(const pdr_net *net, int ncell_sample, const double *d_abundance, const double *d_rate,

@@ -13,6 +13,8 @@
 #include <cmath>
 #include <vector>
 
+#include <mutex>
+
 #include "pdr_internal.h"
 
 namespace pdr {
@@ -323,8 +325,19 @@ int launch_rates(const pdr_net *net, const pdr_phys &ph, int ncell, int nrays, c
                  int *status, int sm_count, cudaStream_t st) {
   const size_t smem = sizeof(RateRow) * (size_t)net->rates.nreac;
   if (smem > 200 * 1024) return PDR_E_NET;
-  cudaError_t e = cudaFuncSetAttribute(rates_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(rates)");
+  // the attribute only grows, so concurrent launches for networks of
+  // different sizes (server lanes) never lower it under each other
+  cudaError_t e = cudaSuccess;
+  {
+    static std::mutex mu;
+    static size_t attr = 0;
+    std::lock_guard<std::mutex> lk(mu);
+    if (smem > attr) {
+      e = cudaFuncSetAttribute(rates_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(rates)");
+      attr = smem;
+    }
+  }
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, rates_kernel, 256, smem);
   if (per_sm < 1) per_sm = 1;

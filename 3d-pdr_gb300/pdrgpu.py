@@ -10,6 +10,8 @@ missing library or GPU raises instead of falling back to the CPU.
 import ctypes as C
 import os
 
+import numpy as np
+
 PKG = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(PKG)
 DATA = os.path.join(ROOT, "data")
@@ -25,7 +27,18 @@ class ChemOpts(C.Structure):
     _fields_ = [("reltol", C.c_double), ("abstol", C.c_double), ("start_time_yr", C.c_double),
                 ("end_time_yr", C.c_double), ("mxstep", C.c_long), ("precision", C.c_int),
                 ("warps_per_block", C.c_int), ("blocks_per_sm", C.c_int), ("reg_variant", C.c_int),
-                ("refill", C.c_int), ("integrator", C.c_int)]
+                ("refill", C.c_int), ("integrator", C.c_int), ("max_sms", C.c_int)]
+
+
+class ServerOpts(C.Structure):
+    _fields_ = [("max_batch_cells", C.c_int), ("nrays", C.c_int), ("precision", C.c_int),
+                ("partition_sms", C.c_int)]
+
+
+class ServeRequest(C.Structure):
+    _fields_ = [("network", C.c_int), ("ncell", C.c_int), ("t_end_yr", C.c_double),
+                ("n_H", C.c_void_p), ("T", C.c_void_p), ("Tdust", C.c_void_p), ("rad_surface", C.c_void_p),
+                ("AV", C.c_void_p), ("column5", C.c_void_p), ("abundance", C.c_void_p), ("status", C.c_void_p)]
 
 
 class Phys(C.Structure):
@@ -77,6 +90,15 @@ def lib():
     L.pdr_levpop_batched.argtypes = [_vp, C.c_int, C.c_int] + [_vp] * 7 + [C.c_int, C.c_double, C.c_double,
                                                                           C.c_int] + [_vp] * 5
     L.pdr_lte_batched.argtypes = [_vp, C.c_int] + [_vp] * 5
+    L.pdr_solver_create.argtypes = [_vp, C.c_int, C.POINTER(ChemOpts), C.POINTER(_vp)]
+    L.pdr_solver_run.argtypes = [_vp, C.c_int] + [_vp] * 7
+    L.pdr_solver_free.argtypes = [_vp]
+    L.pdr_server_opts_default.argtypes = [C.POINTER(ServerOpts)]
+    L.pdr_server_create.argtypes = [C.POINTER(_vp), C.c_int, C.POINTER(Phys), C.POINTER(ServerOpts), C.POINTER(_vp)]
+    L.pdr_server_submit.argtypes = [_vp, C.POINTER(ServeRequest), C.POINTER(C.c_longlong)]
+    L.pdr_server_wait.argtypes = [_vp, C.c_longlong, C.POINTER(C.c_double)]
+    L.pdr_server_stats.argtypes = [_vp, C.c_int, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
+    L.pdr_server_free.argtypes = [_vp]
     _LIB = L
     return L
 
@@ -307,3 +329,78 @@ def autotune(net, abundance, rate, density, opts, ncell_sample=None, stream=None
     check(lib().pdr_chem_autotune(net.handle, n, _ptr(abundance), _ptr(rate), _ptr(density), C.byref(opts),
                                   _stream(stream)), "pdr_chem_autotune")
     return opts
+
+
+class Solver:
+    """A solver instance with its own device scratch (pdr_solver_*): runs
+    allocate nothing; instances on different streams may overlap."""
+
+    def __init__(self, net, max_cells, opts=None):
+        h = _vp()
+        check(lib().pdr_solver_create(net.handle, max_cells, C.byref(opts or chem_opts("mixed")), C.byref(h)),
+              "pdr_solver_create")
+        self.handle, self.net = h, net
+
+    def run(self, abundance, rate, density, t_end_yr=None, status=None, stats=None, stream=None):
+        import torch
+        n = abundance.shape[0]
+        if status is None:
+            status = torch.empty(n, dtype=torch.int32, device=abundance.device)
+        check(lib().pdr_solver_run(self.handle, n, _ptr(abundance), _ptr(rate), _ptr(density),
+                                   _ptr(t_end_yr) if t_end_yr is not None else None, _ptr(status),
+                                   _ptr(stats) if stats is not None else None, _stream(stream)), "pdr_solver_run")
+        return status
+
+    def close(self):
+        if getattr(self, "handle", None) is not None and _LIB is not None:
+            _LIB.pdr_solver_free(self.handle)
+            self.handle = None
+
+    __del__ = close
+
+
+class Server:
+    """The serving loop (pdr_server_*): one lane per network, FIFO continuous
+    batching, everything allocated up front.  Requests are numpy arrays that
+    must stay alive until wait() returns (the object keeps references)."""
+
+    def __init__(self, nets, ph, max_batch_cells=65536, nrays=12, precision="mixed"):
+        o = ServerOpts()
+        lib().pdr_server_opts_default(C.byref(o))
+        o.max_batch_cells, o.nrays = max_batch_cells, nrays
+        o.precision = PDR_MIXED if precision == "mixed" else PDR_FP64
+        arr = (_vp * len(nets))(*[n.handle for n in nets])
+        h = _vp()
+        check(lib().pdr_server_create(arr, len(nets), C.byref(ph), C.byref(o), C.byref(h)), "pdr_server_create")
+        self.handle, self.nets, self.nrays = h, list(nets), nrays
+        self._keep = {}
+
+    def submit(self, network, n_H, T, Tdust, rad_surface, AV, column5, abundance, t_end_yr, status=None):
+        """abundance (ncell, nspec) float64 C-contiguous, overwritten with the result."""
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (n_H, T, Tdust, rad_surface, AV, column5)]
+        assert abundance.flags["C_CONTIGUOUS"] and abundance.dtype == np.float64
+        r = ServeRequest(network, len(arrs[0]), float(t_end_yr), *[a.ctypes.data for a in arrs],
+                         abundance.ctypes.data, status.ctypes.data if status is not None else None)
+        t = C.c_longlong()
+        check(lib().pdr_server_submit(self.handle, C.byref(r), C.byref(t)), "pdr_server_submit")
+        self._keep[t.value] = (arrs, abundance, status, r)
+        return t.value
+
+    def wait(self, ticket):
+        """Returns (result, latency_ms): result 0, the last nonzero cell flag, or a PDR_E_* code."""
+        lat = C.c_double()
+        rc = lib().pdr_server_wait(self.handle, ticket, C.byref(lat))
+        self._keep.pop(ticket, None)
+        return rc, lat.value
+
+    def stats(self, lane):
+        b, c = C.c_longlong(), C.c_longlong()
+        check(lib().pdr_server_stats(self.handle, lane, C.byref(b), C.byref(c)), "pdr_server_stats")
+        return b.value, c.value
+
+    def close(self):
+        if getattr(self, "handle", None) is not None and _LIB is not None:
+            _LIB.pdr_server_free(self.handle)
+            self.handle = None
+
+    __del__ = close

@@ -64,6 +64,8 @@ typedef struct {
   int refill;           /* 0: cells refill from an atomic work queue, 1: static split */
   int integrator;       /* 0: automatic (one warp per cell for 32 ODE species, else
                            one block per cell), 1: warp per cell, 2: block per cell */
+  int max_sms;          /* 0: the persistent grid spans every SM; n > 0: only n SMs'
+                           worth of blocks, leaving the rest to concurrent solves */
 } pdr_chem_opts;
 
 void pdr_chem_opts_default(pdr_chem_opts *opts);
@@ -91,6 +93,58 @@ int pdr_chem_solve_batched(const pdr_net *net, int ncell, double *d_abundance,
                            const double *d_rate, const double *d_density,
                            const double *d_t_end_yr, const pdr_chem_opts *opts, int *d_status,
                            int *d_stats, void *stream);
+
+/* A solver instance with its own device scratch, sized at creation for up to
+ * max_cells cells (no counterpart in the reference: it is what a serving loop
+ * or any caller that overlaps solves on several streams needs).  Runs take the
+ * same arguments as pdr_chem_solve_batched with the instance's options,
+ * allocate nothing, and instances on different streams may overlap; runs of
+ * one instance must not overlap each other. */
+typedef struct pdr_solver pdr_solver;
+int pdr_solver_create(const pdr_net *net, int max_cells, const pdr_chem_opts *opts, pdr_solver **out);
+int pdr_solver_run(pdr_solver *solver, int ncell, double *d_abundance, const double *d_rate,
+                   const double *d_density, const double *d_t_end_yr, int *d_status, int *d_stats,
+                   void *stream);
+void pdr_solver_free(pdr_solver *solver);
+
+/* ---- serving (no counterpart in the reference) ----
+ * A server owns one lane per network (a dispatcher thread, a stream, a solver
+ * instance, pinned staging and device buffers for max_batch_cells cells, all
+ * allocated by pdr_server_create).  Requests are blocks of cells given by
+ * their physical conditions and initial abundances; each lane serves its
+ * network's requests in arrival order, packing every queued request that fits
+ * into one launch (reaction rates, then the batched solve, per-cell end
+ * times).  The arrays of a request must stay valid until pdr_server_wait
+ * returns for its ticket; abundance[ncell*nspec] is overwritten with the
+ * result and status[ncell] (or NULL) receives the cells' CVODE flags. */
+typedef struct pdr_server pdr_server;
+typedef struct {
+  int max_batch_cells;  /* cells per launch per lane, also the largest request (65536) */
+  int nrays;            /* rays per cell in the requests (12)                           */
+  int precision;        /* PDR_MIXED (default) or PDR_FP64                              */
+  int partition_sms;    /* 1 (default): each lane's persistent solve uses an equal share
+                           of the SMs, so lanes run side by side instead of one
+                           network's launch holding every SM; 0: all SMs per launch */
+} pdr_server_opts;
+typedef struct {
+  int network;          /* index into the server's network list                        */
+  int ncell;
+  double t_end_yr;
+  const double *n_H, *T, *Tdust;                   /* [ncell]                          */
+  const double *rad_surface, *AV;                  /* [ncell*nrays]                    */
+  const double *column5;                           /* [ncell*nrays*5]: H2, HD, CO, C, S */
+  double *abundance;                               /* [ncell*nspec] in/out             */
+  int *status;                                     /* [ncell] or NULL                  */
+} pdr_serve_request;
+void pdr_server_opts_default(pdr_server_opts *opts);
+int pdr_server_create(pdr_net *const *nets, int nnet, const pdr_phys *phys, const pdr_server_opts *opts,
+                      pdr_server **out);
+int pdr_server_submit(pdr_server *server, const pdr_serve_request *request, long long *ticket);
+/* blocks until the request is done; returns 0, the last nonzero cell flag, or
+ * a PDR_E_* code; latency_ms (or NULL) receives submit-to-completion time */
+int pdr_server_wait(pdr_server *server, long long ticket, double *latency_ms);
+int pdr_server_stats(pdr_server *server, int lane, long long *batches, long long *cells);
+void pdr_server_free(pdr_server *server);
 
 /* Allocation-free variant of pdr_chem_solve_batched, with no counterpart in
  * the reference.  For callers that cannot call cudaMalloc (device memory owned
