@@ -429,8 +429,14 @@ def main():
         p64 = G.probe_fma_tflops(64, stream)
         p32 = G.probe_fma_tflops(32, stream)
         ach64 = f64 / (ms_kernel * 1e-3) / 1e12
+        # DRAM bytes per cell of the integrator launch, from the ncu capture in
+        # profiles/chem_warp_kernel_reduced_4096cells.md (12.1 MB read, 0 written,
+        # 4,096 cells), scaled to this launch by its cells
+        traffic = (12.102912e6 / 4096.0) * ncell if network == "reduced" else None
         extras["roofline"] = {"bound": "fp64", "achieved": ach64, "peak": p64, "unit": "TFLOP/s",
-                              "frac": ach64 / p64, "traffic": None,
+                              "frac": ach64 / p64, "traffic": traffic,
+                              "traffic_note": "bytes per launch: ncu DRAM read+write per cell x cells",
+                              "algorithmic_bytes": float(ncell) * 8.0 * (2 * net.nspec + net.nreac + 1),
                               "peak_source": "measured by pdr_probe_fma_tflops (FP64 FMA) in this run",
                               "fp32": {"achieved": f32 / (ms_kernel * 1e-3) / 1e12, "peak": p32},
                               "kernel": ("chem_warp_kernel<32,mixed>" if network == "reduced" else
