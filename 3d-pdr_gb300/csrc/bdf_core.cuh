@@ -11,7 +11,7 @@
 // retry rules.  Every thread of the group owns one species (or none); the
 // group type D supplies the collectives and the linear algebra:
 //   bool owns; bool leader();  void sync();
-//   double sum_all(double); double max_all(double);
+//   double sum_all(double); float sum_all(float); double max_all(double);
 //   double rhs(double y_own);  bool setup(double y_own);  double solve(double b_own);
 // Norms are kept squared (the tests compare squares, no sqrt); the step-ratio
 // heuristics eta = 1/((bias*e)^(1/k) + 1e-6) are evaluated in FP32.
@@ -48,10 +48,11 @@ struct CoefShared {
 };
 
 // squared-norm form of eta = 1/((bias*e)^(1/k) + 1e-6) with e2 = e^2 (FP32)
-__device__ __forceinline__ double eta_of(double e2, float bias, int k) {
-  const float v = powf(bias * bias * (float)e2, 0.5f / (float)k);
+__device__ __forceinline__ double eta_of(float e2, float bias, int k) {
+  const float v = powf(bias * bias * e2, 0.5f / (float)k);
   return (double)(1.0f / (v + (float)ADDON));
 }
+__device__ __forceinline__ double eta_of(double e2, float bias, int k) { return eta_of((float)e2, bias, k); }
 
 // 1/x to double precision: FP32 seed and two Newton steps
 __device__ __forceinline__ double rcp_nr(double x) {
@@ -95,27 +96,36 @@ struct ZShared {
   __device__ __forceinline__ double &operator[](int j) const { return p[j * s]; }
 };
 
-template <class D, bool ZSHARED = false>
+// NORM32: the error weights, WRMS norms and the convergence-rate estimate in
+// FP32 (the mixed form).  They only feed threshold tests and step-ratio
+// heuristics, and on GB300 every FP64 warp instruction costs 1/60 of an FP32
+// one; the state, corrections, residuals and Nordsieck updates stay FP64.
+template <class D, bool ZSHARED = false, bool NORM32 = false>
 struct Core {
+  using NT = typename std::conditional<NORM32, float, double>::type;
   __device__ __forceinline__ D &self() { return *static_cast<D *>(this); }
   CoefShared *ws = nullptr;
   // Nordsieck row of this thread's species, weight, correction, work values
   typename std::conditional<ZSHARED, ZShared, ZRow>::type z;
-  double ewt, acor, y, ftmp, tmp;
+  NT ewt;
+  double acor, y, ftmp, tmp;
   // uniform integrator scalars
   double tn, h, hscale, hprime, eta, etamax, saved_tq5, gamma, gammap, inv_gammap, gamrat, gscale, rl1;
-  double crate2, acnrm2;
+  NT crate2, acnrm2;
   double xe_last, rtol, atol;
   int q, qprime, qwait, jcur;
   int nst, nstlp, nfe, nje, nsetups, nni, ncfn, netf;
   long long mxstep, max_total_steps;
 
-  __device__ __forceinline__ double wrms2(double v) {
-    const double t = self().owns ? v * ewt : 0.0;
-    return self().sum_all(t * t) * self().inv_n;
+  __device__ __forceinline__ NT wrms2(double v) {
+    const NT t = self().owns ? (NT)v * ewt : NT(0);
+    return self().sum_all(t * t) * (NT)self().inv_n;
   }
 
-  __device__ __forceinline__ void set_ewt() { ewt = self().owns ? rcp_nr(rtol * fabs(z[0]) + atol) : 0.0; }
+  __device__ __forceinline__ void set_ewt() {
+    if constexpr (NORM32) ewt = self().owns ? __frcp_rn((float)(rtol * fabs(z[0]) + atol)) : 0.0f;
+    else ewt = self().owns ? rcp_nr(rtol * fabs(z[0]) + atol) : 0.0;
+  }
 
   // Pascal-triangle prediction z <- z P (and its inverse), q-specialised
   template <int Q, int SIGN>
@@ -328,8 +338,8 @@ struct Core {
   // 0 solved, 1 convergence failure, 2 failure that sends the cell to the FP64 pass
   __device__ __forceinline__ int nls(bool prev_fail, bool fallback_on_fail) {
     bool call_setup = prev_fail || (nst == 0) || (nst >= nstlp + MSBP) || (fabs(gamrat - 1.0) > DGMAX);
-    const double tq4 = ws->tq[4];
-    const double tq4sq = tq4 * tq4;
+    const NT tq4 = (NT)ws->tq[4];
+    const NT tq4sq = tq4 * tq4;
     const int fail = fallback_on_fail ? 2 : 1;
     for (int attempt = 0; attempt < 2; attempt++) {
       y = z[0];
@@ -339,25 +349,25 @@ struct Core {
         call_setup = false;
       }
       acor = 0.0;
-      double delp2 = 0.0;
+      NT delp2 = 0;
       int mcor = 0;
       bool conv = false;
       for (;;) {
         tmp = gamma * ftmp - (rl1 * z[1] + acor);
         tmp = self().solve(tmp) * gscale;
         nni++;
-        const double del2 = wrms2(tmp);
+        const NT del2 = wrms2(tmp);
         acor += tmp;
         y = z[0] + acor;
-        if (mcor > 0) crate2 = fmax(CRDOWN * CRDOWN * crate2, del2 / delp2);
-        if (del2 * fmin(1.0, crate2) <= tq4sq) {
+        if (mcor > 0) crate2 = fmax(NT(CRDOWN * CRDOWN) * crate2, del2 / delp2);
+        if (del2 * fmin(NT(1), crate2) <= tq4sq) {
           acnrm2 = (mcor == 0) ? del2 : wrms2(acor);
           jcur = 0;
           conv = true;
           break;
         }
         mcor++;
-        if (mcor == MAXCOR || (mcor >= 2 && del2 > RDIV * RDIV * delp2)) break;
+        if (mcor == MAXCOR || (mcor >= 2 && del2 > NT(RDIV * RDIV) * delp2)) break;
         delp2 = del2;
         ftmp = self().rhs(y);
       }
@@ -378,7 +388,7 @@ struct Core {
     const double saved_t = tn;
     int ncf = 0, nef = 0;
     bool prev_fail = false;
-    double dsm2 = 0.0;
+    NT dsm2 = 0;
     if (nst > 0 && hprime != h) {
       if (qprime != q) {
         if (qprime > q) increase_order();
@@ -404,9 +414,9 @@ struct Core {
         rescale();
         continue;
       }
-      const double tq2 = ws->tq[2];
+      const NT tq2 = (NT)ws->tq[2];
       dsm2 = acnrm2 * (tq2 * tq2);
-      if (dsm2 <= 1.0) break;
+      if (dsm2 <= NT(1)) break;
       nef++;
       netf++;
       prev_fail = true;
@@ -476,7 +486,7 @@ struct Core {
           double zq = 0.0;
 #pragma unroll
           for (int j = 0; j <= QMAX; j++) if (j == q) zq = z[j];
-          const double tq1 = ws->tq[1];
+          const NT tq1 = (NT)ws->tq[1];
           etaqm1 = eta_of(wrms2(zq) * (tq1 * tq1), (float)BIAS1, q);
         }
         if (q != QMAX && saved_tq5 != 0.0) {
@@ -485,7 +495,7 @@ struct Core {
           float rp = ratio;
           for (int k = 1; k < L; k++) rp *= ratio;
           const double cquot = (double)(((float)ws->tq[5] / (float)saved_tq5) * rp);
-          const double tq3 = ws->tq[3];
+          const NT tq3 = (NT)ws->tq[3];
           etaqp1 = eta_of(wrms2(acor - cquot * z[QMAX]) * (tq3 * tq3), (float)BIAS3, L + 1);
         }
         // ties keep the current order, then prefer the lower one

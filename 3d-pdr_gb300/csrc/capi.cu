@@ -347,7 +347,10 @@ int pdr_solver_create(const pdr_net *net, int max_cells, const pdr_chem_opts *op
   if (!rc && (e = cudaMalloc(&v->s.redo, sizeof(int) * (size_t)max_cells)) != cudaSuccess)
     rc = cuda_fail(e, "cudaMalloc(solver)");
   if (!rc) v->s.redo_cap = (size_t)max_cells;
-  if (!rc && !uses_warp_path(net, o)) rc = cta_scratch(&v->s, cta_bytes_needed(net, o, v->sms));
+  // scratch for a grid over every SM, so that pdr_solver_set_max_sms may widen it later
+  pdr_chem_opts all = o;
+  all.max_sms = 0;
+  if (!rc && !uses_warp_path(net, o)) rc = cta_scratch(&v->s, cta_bytes_needed(net, all, v->sms));
   if (rc) {
     pdr_solver_free(v);
     return rc;
@@ -365,6 +368,15 @@ int pdr_solver_run(pdr_solver *v, int ncell, double *d_abundance, const double *
   if (ncell == 0) return 0;
   return solve_core(v->net, ncell, d_abundance, d_rate, d_density, d_t_end_yr, v->opts, d_status, d_stats, &v->s,
                     false, v->sms, (cudaStream_t)stream);
+}
+
+int pdr_solver_set_max_sms(pdr_solver *v, int max_sms) {
+  if (!v || max_sms < 0) {
+    set_error("pdr_solver_set_max_sms: invalid argument");
+    return PDR_E_ARG;
+  }
+  v->opts.max_sms = max_sms;
+  return 0;
 }
 
 void pdr_solver_free(pdr_solver *v) {

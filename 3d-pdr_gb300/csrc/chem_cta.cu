@@ -106,6 +106,11 @@ __device__ __forceinline__ double warp_sum(double v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
   return v;
 }
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+  return v;
+}
 __device__ __forceinline__ double warp_max(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(FULL, v, o));
@@ -121,7 +126,7 @@ __device__ __forceinline__ unsigned long long mag_key(double v, bool cand) {
 }
 
 template <bool MIXED>
-struct CtaCell : Core<CtaCell<MIXED>> {
+struct CtaCell : Core<CtaCell<MIXED>, false, MIXED> {
   using MT = typename std::conditional<MIXED, float, double>::type;
   const CtaArgs &A;
   const int tid, lane, warp, nw, n, ld;
@@ -157,6 +162,16 @@ struct CtaCell : Core<CtaCell<MIXED>> {
     if (lane == 0) r[warp] = v;
     __syncthreads();
     double s = 0.0;
+    for (int w = 0; w < nw; w++) s += r[w];
+    return s;
+  }
+  __device__ __forceinline__ float sum_all(float v) {
+    v = warp_sum(v);
+    float *r = reinterpret_cast<float *>(red_d + rbuf * MAXW);
+    rbuf ^= 1;
+    if (lane == 0) r[warp] = v;
+    __syncthreads();
+    float s = 0.0f;
     for (int w = 0; w < nw; w++) s += r[w];
     return s;
   }

@@ -66,6 +66,12 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+  return v;
+}
+
 __device__ __forceinline__ double warp_max(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(FULL, v, o));
@@ -143,7 +149,7 @@ __device__ __forceinline__ MT lu_solve_rows(const MT *a, int ld, int lane, int m
 // One cell integrated by one warp: lane = species = Newton-matrix row.
 // ZSH: Nordsieck rows in shared memory instead of registers.
 template <int NSP, bool MIXED, bool ZSH>
-struct WarpCell : Core<WarpCell<NSP, MIXED, ZSH>, ZSH> {
+struct WarpCell : Core<WarpCell<NSP, MIXED, ZSH>, ZSH, MIXED> {
   using MT = typename std::conditional<MIXED, float, double>::type;
   const ChemArgs &A;
   const int lane;
@@ -163,6 +169,7 @@ struct WarpCell : Core<WarpCell<NSP, MIXED, ZSH>, ZSH> {
   __device__ __forceinline__ bool leader() const { return lane == 0; }
   __device__ __forceinline__ void sync() const { __syncwarp(); }
   __device__ __forceinline__ double sum_all(double v) const { return warp_sum(v); }
+  __device__ __forceinline__ float sum_all(float v) const { return warp_sum(v); }
   __device__ __forceinline__ double max_all(double v) const { return warp_max(v); }
 
   // f(y): returns f_lane, records x_e of this call

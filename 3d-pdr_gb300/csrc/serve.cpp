@@ -11,10 +11,11 @@
 //     takes every queued request of its network, in arrival order, that fits
 //     the remaining batch capacity, packs them into one launch (per-cell end
 //     times) and returns each request's cells when the launch completes;
-//   * lanes of different networks run concurrently on their own streams; by
-//     default each lane's persistent solve spans an equal share of the SMs
-//     (pdr_chem_opts.max_sms), because a persistent launch holds its SMs until
-//     its last cell is done and would otherwise stall the other lane.
+//   * lanes of different networks run concurrently on their own streams.  A
+//     persistent launch holds its SMs until its last cell is done, so by
+//     default a lane's launch spans every SM only when no other lane is
+//     running and an equal share with the running lanes otherwise
+//     (pdr_solver_set_max_sms).
 // Each cell is integrated independently, so a request's results do not depend
 // on what it was batched with.
 #include <algorithm>
@@ -68,7 +69,8 @@ struct pdr_server {
   bool stop = false;
   long long next_ticket = 1;
   std::unordered_map<long long, Req *> reqs;
-  int device = 0;
+  int device = 0, sms = 0;
+  int running = 0;   // lanes with a launch in flight
 };
 
 namespace {
@@ -176,11 +178,17 @@ void lane_loop(pdr_server *s, int li) {
         batch.push_back(L.queue.front());
         L.queue.pop_front();
       }
+      // SM share of this launch: all SMs when the other lanes are idle, else
+      // an equal share with the lanes that are running
+      if (s->opts.partition_sms && s->lanes.size() > 1)
+        pdr_solver_set_max_sms(L.solver, s->running == 0 ? 0 : std::max(1, s->sms / (s->running + 1)));
+      s->running++;
     }
     const int rc = run_batch(s, L, batch);
     const Clock::time_point t = Clock::now();
     {
       std::lock_guard<std::mutex> lk(s->mu);
+      s->running--;
       for (Req *q : batch) {
         if (rc) q->result = rc;
         q->finished = t;
@@ -222,6 +230,7 @@ int pdr_server_create(pdr_net *const *nets, int nnet, const pdr_phys *phys, cons
     return PDR_E_ARG;
   }
   cudaGetDevice(&s->device);
+  cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, s->device);
   s->lanes.resize(nnet);
   int rc = 0;
   for (int i = 0; i < nnet && !rc; i++) {
@@ -235,11 +244,6 @@ int pdr_server_create(pdr_net *const *nets, int nnet, const pdr_phys *phys, cons
     pdr_chem_opts o;
     pdr_chem_opts_default(&o);
     o.precision = s->opts.precision;
-    if (s->opts.partition_sms && nnet > 1) {
-      int sms = 0;
-      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
-      o.max_sms = std::max(1, sms / nnet);
-    }
     rc = pdr_solver_create(L.net, s->opts.max_batch_cells, &o, &L.solver);
   }
   // one warm-up cell per lane: kernel attributes and device tables are set up

@@ -93,6 +93,7 @@ def lib():
     L.pdr_solver_create.argtypes = [_vp, C.c_int, C.POINTER(ChemOpts), C.POINTER(_vp)]
     L.pdr_solver_run.argtypes = [_vp, C.c_int] + [_vp] * 7
     L.pdr_solver_free.argtypes = [_vp]
+    L.pdr_solver_set_max_sms.argtypes = [_vp, C.c_int]
     L.pdr_server_opts_default.argtypes = [C.POINTER(ServerOpts)]
     L.pdr_server_create.argtypes = [C.POINTER(_vp), C.c_int, C.POINTER(Phys), C.POINTER(ServerOpts), C.POINTER(_vp)]
     L.pdr_server_submit.argtypes = [_vp, C.POINTER(ServeRequest), C.POINTER(C.c_longlong)]

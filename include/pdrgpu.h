@@ -105,6 +105,8 @@ int pdr_solver_create(const pdr_net *net, int max_cells, const pdr_chem_opts *op
 int pdr_solver_run(pdr_solver *solver, int ncell, double *d_abundance, const double *d_rate,
                    const double *d_density, const double *d_t_end_yr, int *d_status, int *d_stats,
                    void *stream);
+/* limit the persistent grid of later runs to max_sms SMs' worth of blocks (0: all) */
+int pdr_solver_set_max_sms(pdr_solver *solver, int max_sms);
 void pdr_solver_free(pdr_solver *solver);
 
 /* ---- serving (no counterpart in the reference) ----
@@ -122,9 +124,10 @@ typedef struct {
   int max_batch_cells;  /* cells per launch per lane, also the largest request (65536) */
   int nrays;            /* rays per cell in the requests (12)                           */
   int precision;        /* PDR_MIXED (default) or PDR_FP64                              */
-  int partition_sms;    /* 1 (default): each lane's persistent solve uses an equal share
-                           of the SMs, so lanes run side by side instead of one
-                           network's launch holding every SM; 0: all SMs per launch */
+  int partition_sms;    /* 1 (default): a lane's launch spans every SM when no other
+                           lane is running, else an equal share with the running
+                           lanes, so that one network's persistent launch does not hold
+                           every SM while another network waits; 0: all SMs always */
 } pdr_server_opts;
 typedef struct {
   int network;          /* index into the server's network list                        */
