@@ -163,6 +163,14 @@ int build_coolant_tables(pdr_coolant *c) {
   t.weights = up(c, h.weights, rc);
   t.energies = up(c, h.energies, rc);
   t.line_of_pair = up(c, lop, rc);
+  std::vector<int> rp;
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < i; j++) {
+      const int e = i * n + j, et = j * n + i;
+      if (h.A[e] != 0.0 || h.B[e] != 0.0 || h.A[et] != 0.0 || h.B[et] != 0.0) rp.push_back(e);
+    }
+  t.nrad = (int)rp.size();
+  if (!rp.empty()) t.rad_pairs = up(c, rp, rc);
   return rc;
 }
 

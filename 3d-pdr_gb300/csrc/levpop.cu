@@ -52,29 +52,40 @@ __device__ __forceinline__ void argmax_last(double &v, int &idx) {
   }
 }
 
-// Gauss-Jordan with full pivoting on a (n x n, row stride n) and one rhs b,
-// warp-cooperative; the pivot search reproduces the serial scan's choice
-// (last maximum in row-major order).  Returns false on a singular matrix.
+// Gauss-Jordan with full pivoting on a (n x n, row stride n, n <= 64) and one
+// rhs b, warp-cooperative; the result is the reference's element for element:
+//  * pivot search: the last maximum in row-major order over the unpivoted rows
+//    and columns (the serial scan of GAUSS_JORDAN, solvlevpop.F90:65-174),
+//    lanes striding over the flattened matrix, pivoted columns in a bit mask;
+//  * elimination: every (row, column) element, b as column n, updated by one
+//    lane with the reference's unfused a - a_pivot*dum, so the order in which
+//    lanes take the elements does not matter.
+// dumv is n scratch values.  Returns false on a singular matrix.
 template <class R>
-__device__ bool gauss_jordan(R *a, R *b, int n, int *ipiv, int *indxr, int *indxc, bool unscramble) {
+__device__ bool gauss_jordan(R *a, R *b, int n, R *dumv, int *indxr, int *indxc, bool unscramble) {
   const int lane = threadIdx.x & 31;
-  for (int j = lane; j < n; j += 32) ipiv[j] = 0;
-  __syncwarp();
+  const int nn = n * n, w = n + 1;   // elimination width: n columns and b
+  unsigned long long used = 0ull;
   for (int it = 0; it < n; it++) {
     double best = -1.0;
     int bidx = -1;
-    for (int e = lane; e < n * n; e += 32) {
-      const int j = e / n, k = e - j * n;
-      if (ipiv[j] != 1 && ipiv[k] == 0) {
-        const double v = fabs((double)a[e]);
-        if (v >= best) { best = v; bidx = e; }
+    {
+      int j = 0, k = lane;
+      while (k >= n) { k -= n; j++; }
+      for (int e = lane; e < nn; e += 32) {
+        if (!((used >> j) & 1ull) && !((used >> k) & 1ull)) {
+          const double v = fabs((double)a[e]);
+          if (v >= best) { best = v; bidx = e; }
+        }
+        k += 32;
+        while (k >= n) { k -= n; j++; }
       }
     }
     argmax_last(best, bidx);
     if (bidx < 0) return false;
     const int irow = bidx / n, icol = bidx - irow * n;
     __syncwarp();
-    if (lane == 0) ipiv[icol]++;
+    used |= 1ull << icol;
     if (irow != icol) {
       for (int l = lane; l < n; l += 32) {
         const R d = a[irow * n + l];
@@ -93,17 +104,25 @@ __device__ bool gauss_jordan(R *a, R *b, int n, int *ipiv, int *indxr, int *indx
     __syncwarp();
     for (int l = lane; l < n; l += 32) a[icol * n + l] = a[icol * n + l] * pivinv;
     if (lane == 0) b[icol] = b[icol] * pivinv;
+    // the multipliers, read before any row changes
+    for (int ll = lane; ll < n; ll += 32) dumv[ll] = a[ll * n + icol];
     __syncwarp();
-    for (int ll = lane; ll < n; ll += 32) {
-      if (ll == icol) continue;
-      const R dum = a[ll * n + icol];
-      a[ll * n + icol] = R(0);
-      for (int l = 0; l < n; l++) {
-        if constexpr (sizeof(R) == 8) a[ll * n + l] = __dsub_rn(a[ll * n + l], __dmul_rn(a[icol * n + l], dum));
-        else a[ll * n + l] = __fsub_rn(a[ll * n + l], __fmul_rn(a[icol * n + l], dum));
+    {
+      int ll = 0, l = lane;
+      while (l >= w) { l -= w; ll++; }
+      for (int e = lane; e < n * w; e += 32) {
+        if (ll != icol) {
+          const R dum = dumv[ll];
+          const R pv = (l < n) ? a[icol * n + l] : b[icol];
+          R cur = (l == icol) ? R(0) : ((l < n) ? a[ll * n + l] : b[ll]);
+          if constexpr (sizeof(R) == 8) cur = __dsub_rn(cur, __dmul_rn(pv, dum));
+          else cur = __fsub_rn(cur, __fmul_rn(pv, dum));
+          if (l < n) a[ll * n + l] = cur;
+          else b[ll] = cur;
+        }
+        l += 32;
+        while (l >= w) { l -= w; ll++; }
       }
-      if constexpr (sizeof(R) == 8) b[ll] = __dsub_rn(b[ll], __dmul_rn(b[icol], dum));
-      else b[ll] = __fsub_rn(b[ll], __fmul_rn(b[icol], dum));
     }
     __syncwarp();
   }
@@ -177,10 +196,13 @@ __global__ void __launch_bounds__(256) levpop_kernel(const __grid_constant__ Coo
     // ---- escape probabilities and the radiative terms ----
     const double ngrain = 2.0e-12 * rho * A.metallicity * 100. / A.g2d;
     const double *tau = A.tau + (size_t)cell * C.nlin * A.nrays;
-    for (int e = lane; e < nn; e += 32) {
+    for (int e = lane; e < nn; e += 32) aux[e] = 0.0;
+    __syncwarp();
+    // pairs with no radiative coupling in either direction (A = B = 0) leave
+    // R unchanged and their line term zero: only the radiative pairs are visited
+    for (int pe = lane; pe < C.nrad; pe += 32) {
+      const int e = C.rad_pairs[pe];
       const int i = e / n, j = e - i * n;
-      aux[e] = 0.0;
-      if (j >= i) continue;
       const double f = C.freq[e], Aij = C.A[e];
       const double tmp2 = 2.0 * HP * (f * f * f) / (CL * CL);
       double bb = tmp2 * (1.0 / (exp(HP * f / KB / 2.7) - 1.0));
@@ -249,7 +271,7 @@ __global__ void __launch_bounds__(256) levpop_kernel(const __grid_constant__ Coo
     __syncwarp();
     bool ok, redo = false;
     if constexpr (!MIXED) {
-      ok = gauss_jordan<double>(R, b, n, ipiv, indxr, indxc, false);
+      ok = gauss_jordan<double>(R, b, n, rs, indxr, indxc, false);
       for (int i = lane; i < n; i += 32) x[i] = b[i];
     } else {
       // rows equilibrated by their largest entry, FP32 Gauss-Jordan inverse of
@@ -265,7 +287,7 @@ __global__ void __launch_bounds__(256) levpop_kernel(const __grid_constant__ Coo
       for (int e = lane; e < nn; e += 32) Mf[e] = (float)(R[e] * rs[e / n]);
       for (int i = lane; i < n; i += 32) bf[i] = 0.0f;
       __syncwarp();
-      ok = gauss_jordan<float>(Mf, bf, n, ipiv, indxr, indxc, true);   // Mf := inverse of D M
+      ok = gauss_jordan<float>(Mf, bf, n, reinterpret_cast<float *>(ipiv), indxr, indxc, true);   // Mf := inverse of D M
       __syncwarp();
       for (int i = lane; i < n; i += 32) {
         double s = 0.0;
@@ -312,7 +334,7 @@ __global__ void __launch_bounds__(256) levpop_kernel(const __grid_constant__ Coo
         __syncwarp();
         if (lane == 0) b[n - 1] = dens * 1.0e-8;
         __syncwarp();
-        ok = gauss_jordan<double>(R, b, n, ipiv, indxr, indxc, false);
+        ok = gauss_jordan<double>(R, b, n, rs, indxr, indxc, false);
         for (int i = lane; i < n; i += 32) x[i] = b[i];
         redo = true;
       }
@@ -369,6 +391,10 @@ int launch_levpop(const pdr_coolant *c, const LevArgsHost &h, bool mixed, int sm
   A.density = h.density; A.T = h.T; A.Td = h.Td; A.partner5 = h.partner5; A.cdens = h.cdens;
   A.spop = h.spop; A.tau = h.tau; A.pop = h.pop; A.cooling = h.cooling; A.line = h.line; A.status = h.status;
   const int n = c->dev.nlev;
+  if (n > 64) {   // the Gauss-Jordan pivot mask holds 64 levels
+    set_error("pdr_levpop_batched: coolants with more than 64 levels are not supported");
+    return PDR_E_ARG;
+  }
   const size_t pw = levpop_smem_per_warp(n);
   int wpb = (int)((96 * 1024) / pw);
   if (wpb > 8) wpb = 8;

@@ -90,6 +90,8 @@ struct CoolantTables {
   double *A = nullptr, *B = nullptr, *freq = nullptr, *weights = nullptr;
   double *energies = nullptr;  // [nlev] level energies, erg
   int *line_of_pair = nullptr; // [nlev*nlev] radiative line of (i,j), i>j, else -1
+  int nrad = 0;
+  int *rad_pairs = nullptr;    // [nrad] pairs i*nlev+j, i>j, with A or B nonzero either way
 };
 
 // host-side argument bundle of the level-population launch
