@@ -15,7 +15,7 @@ import numpy as np
 PKG = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(PKG)
 DATA = os.path.join(ROOT, "data")
-LIB_PATH = os.path.join(PKG, "lib3dpdr_gb300.so")
+LIB_PATH = os.environ.get("PDR_LIBRARY") or os.path.join(PKG, "lib3dpdr_gb300.so")
 
 PDR_FP64, PDR_MIXED = 0, 1
 STATUS = {0: "ok", -1: "too much work", -3: "error test failures", -4: "convergence failures"}
