@@ -110,7 +110,8 @@ struct Core {
   NT ewt;
   double acor, y, ftmp, tmp;
   // uniform integrator scalars
-  double tn, h, hscale, hprime, eta, etamax, saved_tq5, gamma, gammap, inv_gammap, gamrat, gscale, rl1;
+  double tn, h, hscale, hprime, eta, etamax, saved_tq5, gamma, gammap, rl1;
+  NT inv_gammap, gamrat, gscale;
   NT crate2, acnrm2;
   double xe_last, rtol, atol;
   int q, qprime, qwait, jcur;
@@ -219,52 +220,56 @@ struct Core {
 
   // Fixed-leading-coefficient BDF coefficients l[0..q] and error constants
   // tq[1..5] for step h and step history tau[1..q] (q+1 for tq[3])
-  __device__ __forceinline__ static void coeffs(int q, bool order_change_due, double h, const double *tau,
-                                                double *l, double *tq) {
+  // T = double, or float in the mixed form: the coefficients only scale the
+  // Newton correction and the error-test thresholds, so FP32 perturbs the
+  // solution by ~1e-7 of the correction (itself of the size of the local
+  // error), and the ~10 divisions here cost FP32 instead of FP64 issue slots
+  template <class T>
+  __device__ __forceinline__ static void coeffs(int q, bool order_change_due, T h, const double *tau, T *l, T *tq) {
 #pragma unroll
-    for (int j = 0; j <= QMAX; j++) l[j] = 0.0;
-    l[0] = l[1] = 1.0;
-    double a0 = -1.0, a0hat = -1.0, xi_inv = 1.0, xistar_inv = 1.0, hsum = h;
+    for (int j = 0; j <= QMAX; j++) l[j] = T(0);
+    l[0] = l[1] = T(1);
+    T a0 = T(-1), a0hat = T(-1), xi_inv = T(1), xistar_inv = T(1), hsum = h;
     if (q > 1) {
 #pragma unroll
       for (int j = 2; j < QMAX; j++) {
         if (j < q) {
-          hsum += tau[j - 1];
+          hsum += (T)tau[j - 1];
           xi_inv = h / hsum;
-          a0 -= 1.0 / j;
+          a0 -= T(1) / T(j);
 #pragma unroll
           for (int i = QMAX; i >= 1; i--)
             if (i <= j) l[i] += l[i - 1] * xi_inv;
         }
       }
-      a0 -= 1.0 / q;
+      a0 -= T(1) / T(q);
       xistar_inv = -l[1] - a0;
-      hsum += tau[q - 1];
+      hsum += (T)tau[q - 1];
       xi_inv = h / hsum;
       a0hat = -l[1] - xi_inv;
 #pragma unroll
       for (int i = QMAX; i >= 1; i--)
         if (i <= q) l[i] += l[i - 1] * xistar_inv;
     }
-    double lq = 0.0;
+    T lq = T(0);
 #pragma unroll
     for (int j = 0; j <= QMAX; j++) if (j == q) lq = l[j];
-    const double A1 = 1.0 - a0hat + a0, A2 = 1.0 + q * A1;
+    const T A1 = T(1) - a0hat + a0, A2 = T(1) + T(q) * A1;
     tq[2] = fabs(A1 / (a0 * A2));
     tq[5] = fabs(A2 * xistar_inv / (lq * xi_inv));
     if (order_change_due) {
       if (q > 1) {
-        const double C = xistar_inv / lq, A3 = a0 + 1.0 / q, A4 = a0hat + xi_inv;
-        tq[1] = fabs(C * (1.0 - A4 + A3) / A3);
+        const T C = xistar_inv / lq, A3 = a0 + T(1) / T(q), A4 = a0hat + xi_inv;
+        tq[1] = fabs(C * (T(1) - A4 + A3) / A3);
       } else {
-        tq[1] = 1.0;
+        tq[1] = T(1);
       }
-      hsum += tau[q];
+      hsum += (T)tau[q];
       xi_inv = h / hsum;
-      const double A5 = a0 - 1.0 / (q + 1), A6 = a0hat - xi_inv;
-      tq[3] = fabs(((1.0 - A6 + A5) / A2) / (xi_inv * (q + 2) * A5));
+      const T A5 = a0 - T(1) / T(q + 1), A6 = a0hat - xi_inv;
+      tq[3] = fabs(((T(1) - A6 + A5) / A2) / (xi_inv * T(q + 2) * A5));
     }
-    tq[4] = NLSCOEF / tq[2];
+    tq[4] = T(NLSCOEF) / tq[2];
   }
 
   // the table of uniform-history coefficients (h = tau_j = 1)
@@ -274,7 +279,7 @@ struct Core {
     for (int j = 0; j < QMAX + 2; j++) one[j] = 1.0;
     for (int qq = 1; qq <= QMAX; qq++) {
       double l[QMAX + 1], tq[6];
-      coeffs(qq, true, 1.0, one, l, tq);
+      coeffs<double>(qq, true, 1.0, one, l, tq);
       self().sync();
       if (self().leader()) {
         for (int j = 0; j <= QMAX; j++) ws->ul[qq][j] = l[j];
@@ -303,23 +308,24 @@ struct Core {
         if (qwait == 1) { ws->tq[1] = ws->utq[q][1]; ws->tq[3] = ws->utq[q][3]; }
       }
     } else {
-      double l[QMAX + 1], tq[6];
-      tq[1] = ws->tq[1];
-      tq[3] = ws->tq[3];
-      coeffs(q, qwait == 1, h, ws->tau, l, tq);
+      NT l[QMAX + 1], tq[6];
+      tq[1] = (NT)ws->tq[1];
+      tq[3] = (NT)ws->tq[3];
+      coeffs<NT>(q, qwait == 1, (NT)h, ws->tau, l, tq);
       if (self().leader()) {
 #pragma unroll
         for (int j = 0; j <= QMAX; j++) ws->l[j] = l[j];
-        ws->tq[0] = 1.0 / l[1];
+        ws->tq[0] = NT(1) / l[1];
         ws->tq[1] = tq[1]; ws->tq[2] = tq[2]; ws->tq[3] = tq[3]; ws->tq[4] = tq[4]; ws->tq[5] = tq[5];
       }
     }
     self().sync();
     rl1 = ws->tq[0];
     gamma = h * rl1;
-    if (nst == 0) { gammap = gamma; inv_gammap = 1.0 / gamma; }
-    gamrat = (nst > 0) ? gamma * inv_gammap : 1.0;
-    gscale = (gamrat != 1.0) ? 2.0 * rcp_nr(1.0 + gamrat) : 1.0;
+    if (nst == 0) { gammap = gamma; inv_gammap = NT(1) / (NT)gamma; }
+    gamrat = (nst > 0) ? (NT)gamma * inv_gammap : NT(1);
+    if constexpr (NORM32) gscale = (gamrat != 1.0f) ? 2.0f * __frcp_rn(1.0f + gamrat) : 1.0f;
+    else gscale = (gamrat != 1.0) ? 2.0 * rcp_nr(1.0 + gamrat) : 1.0;
   }
 
   // called by D::setup after forming the matrix
@@ -329,15 +335,15 @@ struct Core {
     jcur = 1;
     crate2 = 1.0;
     gammap = gamma;
-    inv_gammap = 1.0 / gamma;
-    gamrat = 1.0;
+    inv_gammap = NT(1) / (NT)gamma;
+    gamrat = NT(1);
     gscale = 1.0;
     nstlp = nst;
   }
 
   // 0 solved, 1 convergence failure, 2 failure that sends the cell to the FP64 pass
   __device__ __forceinline__ int nls(bool prev_fail, bool fallback_on_fail) {
-    bool call_setup = prev_fail || (nst == 0) || (nst >= nstlp + MSBP) || (fabs(gamrat - 1.0) > DGMAX);
+    bool call_setup = prev_fail || (nst == 0) || (nst >= nstlp + MSBP) || (fabs(gamrat - NT(1)) > NT(DGMAX));
     const NT tq4 = (NT)ws->tq[4];
     const NT tq4sq = tq4 * tq4;
     const int fail = fallback_on_fail ? 2 : 1;
@@ -352,9 +358,11 @@ struct Core {
       NT delp2 = 0;
       int mcor = 0;
       bool conv = false;
+      const double rz1 = rl1 * z[1];   // fixed during the iteration
       for (;;) {
-        tmp = gamma * ftmp - (rl1 * z[1] + acor);
-        tmp = self().solve(tmp) * gscale;
+        tmp = gamma * ftmp - (rz1 + acor);
+        tmp = self().solve(tmp);
+        if (gscale != NT(1)) tmp *= (double)gscale;
         nni++;
         const NT del2 = wrms2(tmp);
         acor += tmp;
@@ -560,7 +568,7 @@ struct Core {
       qwait = 2;
       etamax = ETAMX1;
       nst = 0;
-    } else if ((tn - tout) * h >= 0.0) {
+    } else if (tn >= tout) {   // h > 0: the integration runs forward
       return 0;
     }
     long long nstloc = 0;
@@ -571,7 +579,7 @@ struct Core {
       if (kf != 0) return kf;
       nstloc++;
       total++;
-      if ((tn - tout) * h >= 0.0) return 0;
+      if (tn >= tout) return 0;
     }
   }
 
