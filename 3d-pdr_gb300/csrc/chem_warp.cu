@@ -352,7 +352,8 @@ __global__ void __launch_bounds__(RegVariant<RV>::threads, RegVariant<RV>::min_b
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nreac = A.nreac;
   // per-warp shared layout
-  const size_t kn_b = (size_t)nreac * 8, scr_b = (size_t)nreac * 16, xs_b = 8 * (NSP + 2);
+  // scr: the fluxes (FP64) or the two Jacobian scatter buffers (MT each)
+  const size_t kn_b = (size_t)nreac * 8, scr_b = (size_t)nreac * (MIXED ? 8 : 16), xs_b = 8 * (NSP + 2);
   const size_t part_b = 8 * (A.tab.nparts + 1);
   constexpr bool ZSH = RegVariant<RV>::zsh;
   const size_t jrow_b = sizeof(MT) * NSP * (NSP + 3), sig_b = 4 * (NSP + 2) + 4 * NSP;
@@ -443,7 +444,7 @@ __global__ void __launch_bounds__(128) eval_kernel(const __grid_constant__ ChemA
 size_t chem_warp_smem_per_warp(int nsp, int nreac, int nparts, bool mixed, bool zshared) {
   auto al = [](size_t x) { return (x + 15) & ~size_t(15); };
   const size_t mt = mixed ? 4 : 8;
-  return al((size_t)nreac * 8) + al((size_t)nreac * 16) + al(8 * (nsp + 2)) + al(8 * (nparts + 1)) +
+  return al((size_t)nreac * 8) + al((size_t)nreac * (mixed ? 8 : 16)) + al(8 * (nsp + 2)) + al(8 * (nparts + 1)) +
          al(mt * nsp * (nsp + 3)) + al(4 * (nsp + 2) + 4 * nsp) +
          al(sizeof(CoefShared) + (zshared ? 8 * (QMAX + 1) * kWarp : 0));
 }
