@@ -115,6 +115,28 @@ def cpu_reference(ncell_sample, seed_cells, threads, cfg="C3"):
     return ncell_sample / dt, dt
 
 
+def replica_seed(cfg, rank):
+    """Replicas: every rank solves its own grid of the configuration's size,
+    seeded by rank (no exchange between ranks on the data path)."""
+    return CONFIGS[cfg]["seed"] + rank
+
+
+def max_over_ranks(ms, world, device=None):
+    """Whole-job time: the slowest rank's (all_reduce MAX over the process group)."""
+    if world <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(ncell_per_rank, world, steps, ms_total):
+    """cell-solves/s of the whole job: all ranks' cells over the slowest rank's time."""
+    return world * ncell_per_rank * steps / (ms_total * 1e-3)
+
+
 def _timed(fn, stream, reps=1):
     import torch
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -166,6 +188,11 @@ def full_network_sample(G, W, dev, stream, n_mixed=2048, n_fp64=1024):
     m = np.abs(b) > 1e-12
     out["accuracy_vs_fp64"] = {"max_rel_err": float((np.abs(a - b)[m] / np.abs(b)[m]).max()),
                                "cells": n_fp64, "species_floor": 1e-12}
+    # CPU oracle on the host cores, first cells of the same grid (bounded sample)
+    ncpu = int(os.environ.get("PDR_CPU_SAMPLE_FULL", "32"))
+    cv, cdt = cpu_reference(ncpu, ncpu, os.cpu_count() or 1, "C2")
+    out["cpu_baseline"] = {"value": cv, "unit": "cell-solves/s", "cores": os.cpu_count() or 1, "kind": "port",
+                           "sample": f"first {ncpu} cells of the C2 grid ({cdt:.1f} s), oracle/ BDF, OpenMP"}
     return out
 
 
@@ -186,6 +213,16 @@ def level_population_grid(G, W, dev, stream):
             spop, lst = G.lte_populations(cool, base[1], dens, stream=stream)
             tau = torch.as_tensor(W.levpop_tau(n, cool.nlin, seed=lp["seed"] + 1), device=dev)
         row = {}
+        # CPU oracle (find_Ccoeff, escape probability, Gauss-Jordan; OpenMP) on the first cells
+        import oracle as O
+        nc = min(n, int(os.environ.get("PDR_CPU_SAMPLE_LEVPOP", "8192")))
+        oc = O.Coolant(key)
+        hin = [t[:nc].cpu().numpy() for t in (base[0], base[1], base[2], base[3], dens, spop, tau)]
+        t0 = time.perf_counter()
+        oc.levpop(*hin[:6], hin[6])
+        cdt = time.perf_counter() - t0
+        row["cpu_baseline"] = {"cells_per_s": nc / cdt, "cores": os.cpu_count() or 1, "kind": "port",
+                               "sample": f"first {nc} cells ({cdt:.2f} s)"}
         for prec in ("fp64", "mixed"):
             f = lambda: G.level_populations(cool, base[0], base[1], base[2], base[3], dens, spop, tau,
                                             precision=prec, stream=stream)
@@ -307,7 +344,7 @@ def main():
     network = CONFIGS[cfg]["network"]
     F_RHS, F_JAC, N = WORK[network]
     ncell = a.ncell or CONFIGS[cfg]["ncell"]
-    w = W.chemistry(cfg, ncell=ncell, seed=CONFIGS[cfg]["seed"] + rank)
+    w = W.chemistry(cfg, ncell=ncell, seed=replica_seed(cfg, rank))
     net = G.Network(network)
     stream = torch.cuda.Stream(device=dev)
     with torch.cuda.stream(stream):
@@ -366,12 +403,8 @@ def main():
         barrier()
     ms_total = e0.elapsed_time(e1)
     ms_kernel = float(np.mean([s.elapsed_time(t) for s, t in ev]))
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms_total], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_total = float(t.item())
-    value = world * ncell * a.steps / (ms_total * 1e-3)
+    ms_total = max_over_ranks(ms_total, world, dev)
+    value = job_rate(ncell, world, a.steps, ms_total)
     st = stats.cpu().numpy().astype(np.float64)
     ab_mixed = ab.cpu().numpy()
     bad = int((status.cpu().numpy() != 0).sum())
