@@ -170,7 +170,22 @@ int build_coolant_tables(pdr_coolant *c) {
       if (h.A[e] != 0.0 || h.B[e] != 0.0 || h.A[et] != 0.0 || h.B[et] != 0.0) rp.push_back(e);
     }
   t.nrad = (int)rp.size();
-  if (!rp.empty()) t.rad_pairs = up(c, rp, rc);
+  if (!rp.empty()) {
+    // escape_probability.F90:66-71 per pair, with the reference's operation
+    // order and its default-REAL literals
+    const double KB = 1.38065040e-16, CL = 2.99792458e+10, HP = 6.62606896e-27;
+    std::vector<double> tmp2(rp.size()), cmb(rp.size()), emis(rp.size());
+    for (size_t k = 0; k < rp.size(); k++) {
+      const double f = h.freq[rp[k]];
+      tmp2[k] = 2.0 * HP * (f * f * f) / (CL * CL);
+      cmb[k] = tmp2[k] * (1.0 / (std::exp(HP * f / KB / 2.7) - 1.0));
+      emis[k] = (double)0.01f * ((double)1.3f * f / 3.0e11);
+    }
+    t.rad_pairs = up(c, rp, rc);
+    t.pair_tmp2 = up(c, tmp2, rc);
+    t.pair_cmb = up(c, cmb, rc);
+    t.pair_emis = up(c, emis, rc);
+  }
   return rc;
 }
 

@@ -42,11 +42,15 @@ struct LevArgs {
   int *status;
 };
 
+// magnitude bit pattern of a value: ordered like |x| for finite values
+__device__ __forceinline__ long long mag_bits(double x) { return __double_as_longlong(x) & 0x7fffffffffffffffll; }
+__device__ __forceinline__ long long mag_bits(float x) { return (long long)(__float_as_int(x) & 0x7fffffff); }
+
 // warp argmax of (value, index) with ties resolved to the larger index
-__device__ __forceinline__ void argmax_last(double &v, int &idx) {
+__device__ __forceinline__ void argmax_last(long long &v, int &idx) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    const double ov = __shfl_xor_sync(FULL, v, o);
+    const long long ov = __shfl_xor_sync(FULL, v, o);
     const int oi = __shfl_xor_sync(FULL, idx, o);
     if (ov > v || (ov == v && oi > idx)) { v = ov; idx = oi; }
   }
@@ -67,14 +71,16 @@ __device__ bool gauss_jordan(R *a, R *b, int n, R *dumv, int *indxr, int *indxc,
   const int nn = n * n, w = n + 1;   // elimination width: n columns and b
   unsigned long long used = 0ull;
   for (int it = 0; it < n; it++) {
-    double best = -1.0;
+    long long best = -1;
     int bidx = -1;
     {
       int j = 0, k = lane;
       while (k >= n) { k -= n; j++; }
       for (int e = lane; e < nn; e += 32) {
         if (!((used >> j) & 1ull) && !((used >> k) & 1ull)) {
-          const double v = fabs((double)a[e]);
+          // |a| compared through its bit pattern (the order of non-negative
+          // IEEE values), on the integer pipe instead of the FP64 one
+          const long long v = mag_bits(a[e]);
           if (v >= best) { best = v; bidx = e; }
         }
         k += 32;
@@ -204,9 +210,11 @@ __global__ void __launch_bounds__(256) levpop_kernel(const __grid_constant__ Coo
       const int e = C.rad_pairs[pe];
       const int i = e / n, j = e - i * n;
       const double f = C.freq[e], Aij = C.A[e];
-      const double tmp2 = 2.0 * HP * (f * f * f) / (CL * CL);
-      double bb = tmp2 * (1.0 / (exp(HP * f / KB / 2.7) - 1.0));
-      const double emis = (2.0 * ngrain) * ((double)0.01f * ((double)1.3f * f / 3.0e11));
+      // per-pair constants (2 h nu^3 / c^2, the 2.7 K background, the dust
+      // emissivity factor) come precomputed with the coolant
+      const double tmp2 = C.pair_tmp2[pe];
+      double bb = C.pair_cmb[pe];
+      const double emis = (2.0 * ngrain) * C.pair_emis[pe];
       bb = bb + tmp2 * (1.0 / (exp(HP * f / KB / Td) - 1.0) * emis);
       double S, beta;
       bool has_line = true;

@@ -92,6 +92,9 @@ struct CoolantTables {
   int *line_of_pair = nullptr; // [nlev*nlev] radiative line of (i,j), i>j, else -1
   int nrad = 0;
   int *rad_pairs = nullptr;    // [nrad] pairs i*nlev+j, i>j, with A or B nonzero either way
+  double *pair_tmp2 = nullptr; // [nrad] 2 h nu^3 / c^2
+  double *pair_cmb = nullptr;  // [nrad] tmp2 / (exp(h nu / k 2.7 K) - 1)
+  double *pair_emis = nullptr; // [nrad] 0.01 (1.3 nu / 3e11), the dust emissivity factor
 };
 
 // host-side argument bundle of the level-population launch
