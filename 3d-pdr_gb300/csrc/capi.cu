@@ -240,7 +240,7 @@ void pdr_chem_opts_default(pdr_chem_opts *o) {
   o->precision = PDR_FP64;
   o->warps_per_block = 0;
   o->blocks_per_sm = 0;
-  o->reg_variant = 2;   // 168 registers, 12 warps per SM: the fastest variant measured on GB300
+  o->reg_variant = -1;  // per precision: the fastest variant measured on GB300
   o->refill = 0;
   o->integrator = 0;
   o->max_sms = 0;

@@ -479,9 +479,11 @@ int launch_chem_warp(const pdr_net *net, int ncell, double *ab, const double *ra
   A.fallback_list = fb_list;
   A.fallback_count = fb_count;
   A.refill_static = (o.refill == 1) ? 1 : 0;
-  const int wpb = o.warps_per_block > 0 ? o.warps_per_block : 4;
+  // defaults, the fastest shapes measured on GB300: mixed 128 registers with
+  // 8-warp blocks (16 warps/SM), FP64 168 registers with 4-warp blocks
+  const int rv = (o.reg_variant >= 0 && o.reg_variant <= 3) ? o.reg_variant : (mixed ? 1 : 2);
+  const int wpb = o.warps_per_block > 0 ? o.warps_per_block : ((rv >= 2) ? 4 : 8);
   if (wpb > 8) return PDR_E_ARG;
-  const int rv = (o.reg_variant >= 0 && o.reg_variant <= 3) ? o.reg_variant : 0;
   if (rv >= 2 && wpb > 4) return PDR_E_ARG;   // those variants launch at most 128 threads per block
   const bool zsh = (rv == 1 || rv == 3);
   const size_t smem = chem_warp_smem_per_warp(32, A.nreac, T.nparts, mixed, zsh) * wpb;

@@ -54,9 +54,11 @@ typedef struct {
   double end_time_yr;   /* end_time (params.dat), used when d_t_end_yr is NULL       */
   long mxstep;          /* max internal steps per output interval (1e7, calculate_abundances.c:111) */
   int precision;        /* PDR_FP64 or PDR_MIXED                                      */
-  int warps_per_block;  /* warp integrator: warps (cells in flight) per block, 1..8; 0: 4 */
+  int warps_per_block;  /* warp integrator: warps (cells in flight) per block, 1..8; 0:
+                           8 (4 for register variants 2 and 3)                        */
   int blocks_per_sm;    /* 0: as many as fit                                          */
-  int reg_variant;      /* warp integrator register budget: 0 as needed (8 warps/SM),
+  int reg_variant;      /* warp integrator register budget (-1, the default: 1 for the
+                           mixed form, 2 for FP64): 0 as needed (8 warps/SM),
                            1 at most 128 per thread (16 warps/SM, Nordsieck rows in
                            shared memory), 2 at most 168 (12 warps/SM), 3 as 2 with
                            the Nordsieck rows in shared memory; 2 and 3 take at most
