@@ -37,6 +37,7 @@ int launch_chem_cta(const pdr_net *net, int ncell, double *ab, const double *rat
                     int *fb_list, int *fb_count, const int *cell_list, const int *total_ptr, bool mixed,
                     int grid, void *scratch, cudaStream_t st);
 size_t chem_cta_global_bytes(const pdr_net *net, bool mixed, int grid);
+size_t chem_cta_smem(const pdr_net *net, bool mixed, bool *mat_smem);
 int chem_cta_blocks_per_sm(const pdr_net *net, bool mixed);
 int launch_rates(const pdr_net *net, const pdr_phys &ph, int ncell, int nrays, const double *T,
                  const double *Td, const double *rad, const double *AV, const double *col5, double *rate,
@@ -194,8 +195,20 @@ static int solve_core(const pdr_net *net, int ncell, double *ab, const double *r
     return launch_chem_warp(net, ncell, ab, rate, dens, tend, o, status, stats, s->counters + 1, nullptr, nullptr,
                             s->redo, s->counters + 2, false, sm_use, st);
   }
-  // one block per cell: persistent grid of SMs x resident blocks
-  const size_t bytes = cta_bytes_needed(net, o, sms);
+  // one block per cell: persistent grid of SMs x resident blocks, or (refill
+  // 2) one block per cell and no persistence, which needs the Newton matrix in
+  // shared memory (the per-block global slots would scale with the cells)
+  const bool one_per_cell = (o.refill == 2);
+  if (one_per_cell) {
+    bool ms = false;
+    chem_cta_smem(net, mixed, &ms);
+    if (!ms) {
+      set_error("pdr: one block per cell (refill 2) needs the Newton matrix in shared memory: use the mixed form");
+      return PDR_E_ARG;
+    }
+  }
+  const int grid_main = one_per_cell ? ncell : cta_grid(net, o, mixed, sms);
+  size_t bytes = std::max(cta_bytes_needed(net, o, sms), chem_cta_global_bytes(net, mixed, grid_main));
   if (grow) {
     rc = cta_scratch(s, bytes);
     if (rc) return rc;
@@ -204,7 +217,7 @@ static int solve_core(const pdr_net *net, int ncell, double *ab, const double *r
     return PDR_E_ARG;
   }
   rc = launch_chem_cta(net, ncell, ab, rate, dens, tend, o, status, stats, s->counters + 0, s->redo, s->counters + 2,
-                       nullptr, nullptr, mixed, cta_grid(net, o, mixed, sms), s->cta, st);
+                       nullptr, nullptr, mixed, grid_main, s->cta, st);
   if (rc || !mixed) return rc;
   return launch_chem_cta(net, ncell, ab, rate, dens, tend, o, status, stats, s->counters + 1, nullptr, nullptr,
                          s->redo, s->counters + 2, false, cta_grid(net, o, false, sms), s->cta, st);

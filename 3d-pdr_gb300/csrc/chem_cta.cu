@@ -684,7 +684,7 @@ int launch_chem_cta(const pdr_net *net, int ncell, double *ab, const double *rat
   A.queue = queue;
   A.fallback_list = fb_list;
   A.fallback_count = fb_count;
-  A.refill_static = (o.refill == 1) ? 1 : 0;
+  A.refill_static = (o.refill == 1 || (o.refill == 2 && !cell_list)) ? 1 : 0;
   bool ms = false;
   const size_t smem = chem_cta_smem(net, mixed, &ms);
   A.kn_global = reinterpret_cast<double *>(scratch);

@@ -478,7 +478,10 @@ int launch_chem_warp(const pdr_net *net, int ncell, double *ab, const double *ra
   A.queue = queue;
   A.fallback_list = fb_list;
   A.fallback_count = fb_count;
-  A.refill_static = (o.refill == 1) ? 1 : 0;
+  // refill 2 (one warp per cell, no persistence) applies to the pass over
+  // all cells; the FP64 pass over a device-side list keeps the work queue
+  const bool one_per_cell = (o.refill == 2) && !cell_list;
+  A.refill_static = (o.refill == 1 || one_per_cell) ? 1 : 0;
   // defaults, the fastest shapes measured on GB300: mixed 128 registers with
   // 8-warp blocks (16 warps/SM), FP64 168 registers with 4-warp blocks
   const int rv = (o.reg_variant >= 0 && o.reg_variant <= 3) ? o.reg_variant : (mixed ? 1 : 2);
@@ -520,7 +523,8 @@ int launch_chem_warp(const pdr_net *net, int ncell, double *ab, const double *ra
   }
   if (o.blocks_per_sm > 0 && o.blocks_per_sm < per_sm) per_sm = o.blocks_per_sm;
   if (per_sm < 1) per_sm = 1;
-  kernels[variant]<<<sm_count * per_sm, wpb * 32, smem, st>>>(A, ncell, total_ptr);
+  const int grid = one_per_cell ? (ncell + wpb - 1) / wpb : sm_count * per_sm;
+  kernels[variant]<<<grid, wpb * 32, smem, st>>>(A, ncell, total_ptr);
   e = cudaGetLastError();
   return e == cudaSuccess ? 0 : cuda_fail(e, "chem_warp_kernel launch");
 }

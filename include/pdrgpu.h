@@ -63,7 +63,10 @@ typedef struct {
                            shared memory), 2 at most 168 (12 warps/SM), 3 as 2 with
                            the Nordsieck rows in shared memory; 2 and 3 take at most
                            4 warps per block                                          */
-  int refill;           /* 0: cells refill from an atomic work queue, 1: static split */
+  int refill;           /* 0: persistent grid, cells refill from an atomic work queue;
+                           1: persistent grid, static split; 2: one warp (block) per
+                           cell, no persistence (the block integrator needs the mixed
+                           form for this)                                          */
   int integrator;       /* 0: automatic (one warp per cell for 32 ODE species, else
                            one block per cell), 1: warp per cell, 2: block per cell */
   int max_sms;          /* 0: the persistent grid spans every SM; n > 0: only n SMs'
