@@ -47,6 +47,11 @@ int launch_chem_eval(const pdr_net *net, int nstate, const double *x, const doub
 int upload_shield_tables(int dev);
 int build_coolant_tables(pdr_coolant *c);
 int launch_levpop(const pdr_coolant *c, const LevArgsHost &h, bool mixed, int sm_count, cudaStream_t st);
+int launch_uvfield(const pdr_rays &r, const double *rho, int field, const double *G, const double *vectors,
+                   double metallicity, double *colden, double *AV, double *rad, double *uv, int sm_count,
+                   cudaStream_t st);
+int launch_columns(const pdr_rays &r, const double *rho, const double *ab, int nspec, const int *species, int nsel,
+                   double *out, int sm_count, cudaStream_t st);
 int launch_lte(const pdr_coolant *c, int ncell, const double *T, const double *density, double *pop, int *status,
                int sm_count, cudaStream_t st);
 int launch_heating(const pdr_net *net, int network, const pdr_phys &ph, int ncell, const double *dens,
@@ -552,6 +557,41 @@ int pdr_lte_batched(const pdr_coolant *c, int ncell, const double *d_T, const do
   int rc = current_device(&dev, &sms);
   if (rc) return rc;
   return launch_lte(c, ncell, d_T, d_density, d_pop, d_status, sms, (cudaStream_t)stream);
+}
+
+static bool rays_ok(const pdr_rays *r) {
+  return r && r->ncell >= 0 && r->nrays > 0 && r->ngrid > 0 &&
+         (r->ncell == 0 || (r->d_epray && r->d_offset && r->d_xyz && r->d_gridpoint));
+}
+
+int pdr_uvfield_batched(const pdr_rays *rays, const double *d_rho, int field, const double *G, const double *vectors,
+                        double metallicity, double *d_columndensity, double *d_AV, double *d_rad_surface,
+                        double *d_uvfield, void *stream) {
+  if (!rays_ok(rays) || !d_rho || !G || (field != 0 && field != 1) || (field == 1 && !vectors) ||
+      !d_columndensity || !d_AV || !d_rad_surface || !d_uvfield) {
+    set_error("pdr_uvfield_batched: invalid argument");
+    return PDR_E_ARG;
+  }
+  if (rays->ncell == 0) return 0;
+  int dev = 0, sms = 0;
+  int rc = current_device(&dev, &sms);
+  if (rc) return rc;
+  return launch_uvfield(*rays, d_rho, field, G, vectors, metallicity, d_columndensity, d_AV, d_rad_surface,
+                        d_uvfield, sms, (cudaStream_t)stream);
+}
+
+int pdr_column_densities_batched(const pdr_rays *rays, const double *d_rho, const double *d_abundance, int nspec,
+                                 const int *species, int nsel, double *d_columns, void *stream) {
+  if (!rays_ok(rays) || !d_rho || !d_abundance || nspec <= 0 || nsel <= 0 || nsel > 256 ||
+      (!species && nsel > nspec) || !d_columns) {
+    set_error("pdr_column_densities_batched: invalid argument");
+    return PDR_E_ARG;
+  }
+  if (rays->ncell == 0) return 0;
+  int dev = 0, sms = 0;
+  int rc = current_device(&dev, &sms);
+  if (rc) return rc;
+  return launch_columns(*rays, d_rho, d_abundance, nspec, species, nsel, d_columns, sms, (cudaStream_t)stream);
 }
 
 int pdr_heating_batched(const pdr_net *net, int network, const pdr_phys *phys, int ncell, const double *d_density,

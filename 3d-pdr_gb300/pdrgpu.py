@@ -41,6 +41,12 @@ class ServeRequest(C.Structure):
                 ("AV", C.c_void_p), ("column5", C.c_void_p), ("abundance", C.c_void_p), ("status", C.c_void_p)]
 
 
+class Rays(C.Structure):
+    _fields_ = [("ncell", C.c_int), ("nrays", C.c_int), ("ngrid", C.c_int), ("npoint", C.c_longlong),
+                ("d_epray", C.c_void_p), ("d_offset", C.c_void_p), ("d_xyz", C.c_void_p),
+                ("d_gridpoint", C.c_void_p)]
+
+
 class Phys(C.Structure):
     _fields_ = [("zeta", C.c_double), ("omega", C.c_double), ("grain_radius", C.c_double),
                 ("metallicity", C.c_double), ("g2d", C.c_double), ("v_turb", C.c_double),
@@ -90,6 +96,10 @@ def lib():
     L.pdr_levpop_batched.argtypes = [_vp, C.c_int, C.c_int] + [_vp] * 7 + [C.c_int, C.c_double, C.c_double,
                                                                           C.c_int] + [_vp] * 5
     L.pdr_lte_batched.argtypes = [_vp, C.c_int] + [_vp] * 5
+    L.pdr_uvfield_batched.argtypes = [C.POINTER(Rays), _vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                      C.c_double, _vp, _vp, _vp, _vp, _vp]
+    L.pdr_column_densities_batched.argtypes = [C.POINTER(Rays), _vp, _vp, C.c_int, C.POINTER(C.c_int), C.c_int,
+                                               _vp, _vp]
     L.pdr_solver_create.argtypes = [_vp, C.c_int, C.POINTER(ChemOpts), C.POINTER(_vp)]
     L.pdr_solver_run.argtypes = [_vp, C.c_int] + [_vp] * 7
     L.pdr_solver_free.argtypes = [_vp]
@@ -405,3 +415,41 @@ class Server:
             self.handle = None
 
     __del__ = close
+
+
+def device_rays(r, device):
+    """Upload workloads.rays()-style evaluation points; returns (Rays, tensors kept alive)."""
+    import torch
+    t = dict(epray=torch.as_tensor(np.ascontiguousarray(r["epray"], dtype=np.int32), device=device),
+             offset=torch.as_tensor(np.ascontiguousarray(r["offset"], dtype=np.int64), device=device),
+             xyz=torch.as_tensor(np.ascontiguousarray(r["xyz"], dtype=np.float64), device=device),
+             gridpoint=torch.as_tensor(np.ascontiguousarray(r["gridpoint"], dtype=np.int32), device=device))
+    rr = Rays(r["ncell"], r["nrays"], r["ngrid"], r["npoint"], t["epray"].data_ptr(), t["offset"].data_ptr(),
+              t["xyz"].data_ptr(), t["gridpoint"].data_ptr())
+    return rr, t
+
+
+def uvfield(rays, rho, field, G, vectors, metallicity=1.0, stream=None):
+    """CALC_UVFIELD on the device: (columndensity, AV, rad_surface) (ncell, nrays) and UVfield (ncell,)."""
+    import torch
+    n, nr = rays.ncell, rays.nrays
+    out = [torch.empty((n, nr), dtype=torch.float64, device=rho.device) for _ in range(3)]
+    uv = torch.empty(n, dtype=torch.float64, device=rho.device)
+    g = (C.c_double * 3)(*[float(x) for x in G])
+    vec = np.ascontiguousarray(vectors, dtype=np.float64).ravel()
+    check(lib().pdr_uvfield_batched(C.byref(rays), _ptr(rho), field, g, vec.ctypes.data_as(C.POINTER(C.c_double)),
+                                    metallicity, _ptr(out[0]), _ptr(out[1]), _ptr(out[2]), _ptr(uv),
+                                    _stream(stream)), "pdr_uvfield_batched")
+    return out[0], out[1], out[2], uv
+
+
+def column_densities(rays, rho, abundance, species=None, stream=None):
+    """calc_columndens on the device: (ncell, nrays, nsel) columns of the selected species."""
+    import torch
+    nspec = abundance.shape[1]
+    sp = None if species is None else (C.c_int * len(species))(*[int(k) for k in species])
+    nsel = nspec if species is None else len(species)
+    out = torch.empty((rays.ncell, rays.nrays, nsel), dtype=torch.float64, device=rho.device)
+    check(lib().pdr_column_densities_batched(C.byref(rays), _ptr(rho), _ptr(abundance), nspec, sp, nsel, _ptr(out),
+                                             _stream(stream)), "pdr_column_densities_batched")
+    return out

@@ -117,3 +117,46 @@ def serve_stream(nreq, seed=1005, rate_hz=200.0):
     seeds = rng.integers(0, 2**31 - 1, nreq)
     return [dict(arrival=float(a), ncell=int(s), network=str(nw), t_end_yr=float(t), seed=int(sd))
             for a, s, nw, t, sd in zip(arrival, size, network, t_end, seeds)]
+
+
+def healpix_base_directions():
+    """The 12 ray directions of a level-0 HEALPix sphere (nside 1, 3DPDR.F90:311-333):
+    the base-pixel centres, nested order: z = 2/3 north ring, z = 0 equator,
+    z = -2/3 south ring, four azimuths each."""
+    v = []
+    for ring, z in ((0, 2.0 / 3.0), (1, 0.0), (2, -2.0 / 3.0)):
+        for k in range(4):
+            phi = (k + (0.0 if ring == 1 else 0.5)) * np.pi / 2.0
+            s = np.sqrt(1.0 - z * z)
+            v.append((s * np.cos(phi), s * np.sin(phi), z))
+    return np.array(v)
+
+
+def rays(n=8, maxpoints=12, spacing_pc=0.05, step_pc=0.05, nspec=33, seed=1007):
+    """Evaluation points of every cell of an n^3 lattice along the 12 HEALPix
+    directions: points march from the cell in steps of step_pc until they leave
+    the lattice or reach maxpoints, each projected to its nearest lattice point
+    (3D-PDR's ray tracing records the same kind of lists).  Stored padded:
+    ray (c, j) starts at point (c*12 + j)*(maxpoints + 1), point 0 is the cell.
+    Grid densities n_H ~ logU(1e2, 1e5), abundances ~ logU(1e-12, 1e-2)
+    (seeded, stated)."""
+    rng = _rng(seed)
+    d = healpix_base_directions()
+    nrays = len(d)
+    ii, jj, kk = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
+    lat = np.stack([ii.ravel(), jj.ravel(), kk.ravel()], axis=-1).astype(np.float64)   # lattice coords
+    ncell = len(lat)
+    steps = np.arange(maxpoints + 1, dtype=np.float64) * (step_pc / spacing_pc)
+    # positions in lattice units: (ncell, nrays, maxpoints+1, 3)
+    pos = lat[:, None, None, :] + steps[None, None, :, None] * d[None, :, None, :]
+    inside = np.all((pos >= -0.5) & (pos <= n - 0.5), axis=-1)
+    epray = (np.cumprod(inside, axis=-1).sum(axis=-1) - 1).astype(np.int32)   # points after the cell
+    proj = np.clip(np.rint(pos), 0, n - 1).astype(np.int64)
+    gp = (proj[..., 0] * n * n + proj[..., 1] * n + proj[..., 2]).astype(np.int32)
+    xyz = pos * spacing_pc
+    offset = (np.arange(ncell * nrays, dtype=np.int64) * (maxpoints + 1))
+    rho = 10.0 ** rng.uniform(2.0, 5.0, ncell)
+    ab = 10.0 ** rng.uniform(-12.0, -2.0, (ncell, nspec))
+    return dict(ncell=ncell, nrays=nrays, ngrid=ncell, npoint=ncell * nrays * (maxpoints + 1),
+                epray=epray.reshape(-1), offset=offset, xyz=xyz.reshape(-1, 3), gridpoint=gp.reshape(-1),
+                rho=rho, abundance=ab, vectors=d)

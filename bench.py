@@ -308,6 +308,40 @@ def served_stream(G, W, nreq=24, nreq_reduced=64):
     return out
 
 
+def ray_columns_grid(G, W, dev, stream, n=64, maxpoints=12):
+    """The step before the rates (CALC_UVFIELD and calc_columndens, 3DPDR.F90:
+    1636-1844) on a 64^3 lattice: every cell's 12 HEALPix rays with up to 12
+    evaluation points each; total-H columns, A_V and the attenuated field, plus
+    the columns of the 5 species the rates read."""
+    import torch
+    r = W.rays(n, maxpoints, nspec=33, seed=1008)
+    rays, keep = G.device_rays(r, dev)
+    rho = torch.as_tensor(r["rho"], device=dev)
+    ab = torch.as_tensor(r["abundance"], device=dev)
+    sel = [0, 5, 12, 20, 31]
+    f = lambda: (G.uvfield(rays, rho, 0, (10.0, 0.0, 0.0), r["vectors"], stream=stream),
+                 G.column_densities(rays, rho, ab, sel, stream=stream))
+    with torch.cuda.stream(stream):
+        f()
+        ms = _timed(f, stream, 5)
+    npts = int(r["epray"].sum())
+    # algorithmic bytes: per visited point (both passes) coordinates, grid index,
+    # density and 5 abundances; per ray its count and offset; the outputs
+    bytes_ = npts * (2 * (24 + 4 + 8) + 5 * 8) + r["ncell"] * 12 * (2 * 12 + 3 * 8 + 5 * 8) + r["ncell"] * 8
+    ncpu = min(r["ncell"], int(os.environ.get("PDR_CPU_SAMPLE_RAYS", "32768")))
+    import oracle as O
+    sub = dict(r, ncell=ncpu)
+    t0 = time.perf_counter()
+    O.uvfield(sub)
+    O.columns(sub, sel)
+    cdt = time.perf_counter() - t0
+    return {"workload": f"{n}^3 lattice, 12 rays, <= {maxpoints} evaluation points per ray "
+                        f"({npts} points visited), 5 species columns + UV field",
+            "ms": ms, "cells_per_s": r["ncell"] / (ms * 1e-3), "algorithmic_GBps": bytes_ / (ms * 1e-3) / 1e9,
+            "cpu_baseline": {"cells_per_s": ncpu / cdt, "cores": os.cpu_count() or 1, "kind": "port",
+                             "sample": f"first {ncpu} cells ({cdt:.2f} s)"}}
+
+
 def run_reference(a, rank):
     if rank != 0:
         return
@@ -499,7 +533,8 @@ def main():
         if cfg == "C3" and not a.no_secondary:
             extras["secondary"] = {"C2": full_network_sample(G, W, dev, stream),
                                    "C4": level_population_grid(G, W, dev, stream),
-                                   "C5": served_stream(G, W)}
+                                   "C5": served_stream(G, W),
+                                   "rays": ray_columns_grid(G, W, dev, stream)}
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "cell-solves/s", "n_gpus": world, "steps": a.steps,
                 "warmup": a.warmup, "ms_per_step": ms_total / a.steps, "higher_is_better": True,

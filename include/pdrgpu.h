@@ -241,6 +241,44 @@ int pdr_levpop_batched(const pdr_coolant *c, int ncell, int nrays, const double 
 int pdr_lte_batched(const pdr_coolant *c, int ncell, const double *d_T, const double *d_density, double *d_pop,
                     int *d_status, void *stream);
 
+/* ---- rays: column densities and the UV field (3DPDR.F90:1636-1844) ----
+ * The evaluation points of every (cell, ray), as the ray tracing leaves them
+ * (pdr%epray, pdr%epoint, pdr%projected; 3DPDR.F90:346-350), flattened: the
+ * points i = 0..epray of cell c's ray j are d_offset[c*nrays+j] + i in d_xyz
+ * (x, y, z per point) and d_gridpoint (index of the grid point projected there,
+ * into the grid arrays d_rho and d_abundance); point 0 is the cell itself.
+ * epray = 0 is a ray with no evaluation points.  ngrid bounds the grid
+ * indices: a ray that refers to a grid point outside [0, ngrid) gets NaN
+ * results instead of reading outside the grid arrays. */
+typedef struct {
+  int ncell, nrays, ngrid;
+  long long npoint;           /* length of the point arrays; rays reaching past it give NaN */
+  const int *d_epray;         /* [ncell*nrays] */
+  const long long *d_offset;  /* [ncell*nrays] */
+  const double *d_xyz;        /* [npoint*3] */
+  const int *d_gridpoint;     /* [npoint] */
+} pdr_rays;
+
+/* CALC_UVFIELD (3DPDR.F90:1636-1701) for every cell: the total-H column along
+ * each ray, sum over points of (rho_{i-1} + rho_i)/2 * |x_i - x_{i-1}| * pc
+ * (d_columndensity[ncell*nrays]), A_V = column * 6.289e-22 * metallicity
+ * (d_AV), the surface field per ray (d_rad_surface; field 0 "ISO": G0/nrays,
+ * field 1 "UNI": -G.v on the ray most anti-parallel to G, vectors[3*nrays] the
+ * ray directions, host memory) and the attenuated field sum_j rad_j
+ * exp(-3.02 A_V,j) with the reference's clamp of values below 1e-50 to 0 after
+ * each ray (d_uvfield[ncell]).  G[3] on the host: G0 for "ISO" is G[0]. */
+int pdr_uvfield_batched(const pdr_rays *rays, const double *d_rho, int field, const double *G,
+                        const double *vectors, double metallicity, double *d_columndensity, double *d_AV,
+                        double *d_rad_surface, double *d_uvfield, void *stream);
+
+/* calc_columndens (3DPDR.F90:1789-1844): d_columns[(c*nrays+j)*nsel+s] = sum over
+ * the points of ray j of |x_i - x_{i-1}| * pc * (rho_{i-1} x_{i-1,k} + rho_i x_{i,k})/2
+ * for the species k = species[s] (host array of nsel <= 256 indices; NULL: the
+ * first nsel species in order), x from d_abundance[gridpoint*nspec+k].  The
+ * rates need k = H2, HD, CO, C, S in that order (their column5 argument). */
+int pdr_column_densities_batched(const pdr_rays *rays, const double *d_rho, const double *d_abundance,
+                                 int nspec, const int *species, int nsel, double *d_columns, void *stream);
+
 /* ---- heating: batched CALC_HEATING (sub_calculate_heating.F90:7-386) ----
  * network 0 = reduced, 1 = full (the reference's compile-time choice of the
  * chemical-heating reactions); d_abundance[ncell*nspec] and d_rate[ncell*nreac]

@@ -98,6 +98,10 @@ def _load():
     lib.orc_lte.argtypes = [C.POINTER(OrcCoolant), C.c_double, C.c_double, _dp]
     lib.orc_heating.argtypes = [C.POINTER(OrcNet), C.c_int, C.POINTER(OrcPhys), C.c_double,
                                 C.c_double, C.c_double, C.c_double, _dp, _dp, _ip, _dp]
+    _lp64 = C.POINTER(C.c_longlong)
+    lib.orc_uvfield.argtypes = [C.c_int, C.c_int, _ip, _lp64, _dp, _ip, _dp, C.c_int, _dp, _dp, C.c_double,
+                                _dp, _dp, _dp, _dp]
+    lib.orc_columns.argtypes = [C.c_int, C.c_int, _ip, _lp64, _dp, _ip, _dp, _dp, C.c_int, _ip, C.c_int, _dp]
     return lib
 
 
@@ -278,3 +282,36 @@ class RefNetwork:
         J = np.zeros((neq, neq))  # column-major from the reference: J[j, i]
         self.lib.ref_jac(neq, _ptr(x), _ptr(J), _ptr(rate), n_H, T, x_e)
         return J.T.copy()
+
+
+def _rays_arrays(r):
+    return (np.ascontiguousarray(r["epray"], dtype=np.int32), np.ascontiguousarray(r["offset"], dtype=np.int64),
+            np.ascontiguousarray(r["xyz"], dtype=np.float64), np.ascontiguousarray(r["gridpoint"], dtype=np.int32))
+
+
+def uvfield(r, field=0, G=(10.0, 0.0, 0.0), metallicity=1.0):
+    """CALC_UVFIELD over the rays of workloads.rays(): (columndensity, AV, rad_surface, UVfield)."""
+    ep, off, xyz, gp = _rays_arrays(r)
+    n, nr = r["ncell"], r["nrays"]
+    col, av, rad, uv = np.zeros(n * nr), np.zeros(n * nr), np.zeros(n * nr), np.zeros(n)
+    g = np.ascontiguousarray(G, dtype=np.float64)
+    vec = np.ascontiguousarray(r["vectors"], dtype=np.float64)
+    rho = np.ascontiguousarray(r["rho"], dtype=np.float64)
+    lib().orc_uvfield(n, nr, _ptr(ep, _ip), off.ctypes.data_as(C.POINTER(C.c_longlong)), _ptr(xyz), _ptr(gp, _ip),
+                      _ptr(rho), field, _ptr(g), _ptr(vec), metallicity, _ptr(col), _ptr(av), _ptr(rad), _ptr(uv))
+    return col.reshape(n, nr), av.reshape(n, nr), rad.reshape(n, nr), uv
+
+
+def columns(r, species=None):
+    """calc_columndens over the rays of workloads.rays(): (ncell, nrays, nsel)."""
+    ep, off, xyz, gp = _rays_arrays(r)
+    n, nr = r["ncell"], r["nrays"]
+    ab = np.ascontiguousarray(r["abundance"], dtype=np.float64)
+    nspec = ab.shape[1]
+    sp = None if species is None else np.ascontiguousarray(species, dtype=np.int32)
+    nsel = nspec if sp is None else len(sp)
+    out = np.zeros(n * nr * nsel)
+    rho = np.ascontiguousarray(r["rho"], dtype=np.float64)
+    lib().orc_columns(n, nr, _ptr(ep, _ip), off.ctypes.data_as(C.POINTER(C.c_longlong)), _ptr(xyz), _ptr(gp, _ip),
+                      _ptr(rho), _ptr(ab), nspec, _ptr(sp, _ip) if sp is not None else None, nsel, _ptr(out))
+    return out.reshape(n, nr, nsel)

@@ -165,6 +165,13 @@ int orc_solvlevpop(int nlev, const double *transition, double density, double *s
 int orc_gauss_jordan(double *a, int n, double *b);
 void orc_lte(const orc_coolant *c, double T, double density, double *pop);
 
+/* orc_rays.c: CALC_UVFIELD and calc_columndens over flattened evaluation points */
+void orc_uvfield(int ncell, int nrays, const int *epray, const long long *offset, const double *xyz, const int *gp,
+                 const double *rho, int field, const double *G, const double *vectors, double metallicity,
+                 double *colden, double *AV, double *rad, double *uv);
+void orc_columns(int ncell, int nrays, const int *epray, const long long *offset, const double *xyz, const int *gp,
+                 const double *rho, const double *ab, int nspec, const int *species, int nsel, double *out);
+
 /* whole per-cell level-population step for one coolant */
 int orc_levpop_batched(const orc_coolant *c, int ncell, const double *density, const double *T,
                        const double *Tdust, const double *partner5, const double *coolant_density,
