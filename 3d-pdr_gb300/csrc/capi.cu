@@ -47,6 +47,8 @@ int launch_chem_eval(const pdr_net *net, int nstate, const double *x, const doub
 int upload_shield_tables(int dev);
 int build_coolant_tables(pdr_coolant *c);
 int launch_levpop(const pdr_coolant *c, const LevArgsHost &h, bool mixed, int sm_count, cudaStream_t st);
+int launch_tau(const pdr_coolant *cool, const pdr_rays &r, const double *pop, const double *T, double v_turb,
+               double *tau, int sm_count, cudaStream_t st);
 int launch_uvfield(const pdr_rays &r, const double *rho, int field, const double *G, const double *vectors,
                    double metallicity, double *colden, double *AV, double *rad, double *uv, int sm_count,
                    cudaStream_t st);
@@ -592,6 +594,19 @@ int pdr_column_densities_batched(const pdr_rays *rays, const double *d_rho, cons
   int rc = current_device(&dev, &sms);
   if (rc) return rc;
   return launch_columns(*rays, d_rho, d_abundance, nspec, species, nsel, d_columns, sms, (cudaStream_t)stream);
+}
+
+int pdr_optical_depths_batched(const pdr_coolant *c, const pdr_rays *rays, const double *d_pop, const double *d_T,
+                               double v_turb, double *d_tau, void *stream) {
+  if (!c || !rays_ok(rays) || !d_pop || !d_T || !d_tau || !(v_turb >= 0.0)) {
+    set_error("pdr_optical_depths_batched: invalid argument");
+    return PDR_E_ARG;
+  }
+  if (rays->ncell == 0 || c->dev.nlin == 0) return 0;
+  int dev = 0, sms = 0;
+  int rc = current_device(&dev, &sms);
+  if (rc) return rc;
+  return launch_tau(c, *rays, d_pop, d_T, v_turb, d_tau, sms, (cudaStream_t)stream);
 }
 
 int pdr_heating_batched(const pdr_net *net, int network, const pdr_phys *phys, int ncell, const double *d_density,

@@ -169,6 +169,19 @@ int build_coolant_tables(pdr_coolant *c) {
       const int e = i * n + j, et = j * n + i;
       if (h.A[e] != 0.0 || h.B[e] != 0.0 || h.A[et] != 0.0 || h.B[et] != 0.0) rp.push_back(e);
     }
+  {
+    // escape_probability.F90:61 per radiative line (FRAC1 of the tau sum)
+    const double CLc = 2.99792458e+10, PIc = 3.141592653589793238462643383279502884197;
+    std::vector<double> f1(h.nlin);
+    for (int l = 0; l < h.nlin; l++) {
+      const int e = h.line_up[l] * n + h.line_lo[l];
+      const double fr = h.freq[e];
+      f1[l] = (h.A[e] * (CLc * CLc * CLc)) / (8.0 * PIc * (fr * fr * fr));
+    }
+    t.line_up = up(c, h.line_up, rc);
+    t.line_lo = up(c, h.line_lo, rc);
+    t.line_frac1 = up(c, f1, rc);
+  }
   t.nrad = (int)rp.size();
   if (!rp.empty()) {
     // escape_probability.F90:66-71 per pair, with the reference's operation

@@ -95,6 +95,8 @@ struct CoolantTables {
   double *pair_tmp2 = nullptr; // [nrad] 2 h nu^3 / c^2
   double *pair_cmb = nullptr;  // [nrad] tmp2 / (exp(h nu / k 2.7 K) - 1)
   double *pair_emis = nullptr; // [nrad] 0.01 (1.3 nu / 3e11), the dust emissivity factor
+  int *line_up = nullptr, *line_lo = nullptr;   // [nlin] levels of each radiative line
+  double *line_frac1 = nullptr;                 // [nlin] A c^3 / (8 pi nu^3)
 };
 
 // host-side argument bundle of the level-population launch

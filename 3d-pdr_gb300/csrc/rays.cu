@@ -139,7 +139,114 @@ __global__ void columns_kernel(const __grid_constant__ ColArgs A) {
   }
 }
 
+struct TauArgs {
+  int ncell, nrays, ngrid, nlev, nlin;
+  long long npoint;
+  const int *epray;
+  const long long *offset;
+  const double *xyz;
+  const int *gp;
+  const double *pop, *T, *weights, *frac1;
+  const int *up, *lo;
+  double v2;
+  double *tau;
+};
+
+// one warp per (cell, ray), lanes over the radiative lines
+__global__ void tau_kernel(const __grid_constant__ TauArgs A) {
+  constexpr double KB = 1.38065040e-16, MP = 1.67262164e-24, PI = 3.141592653589793238462643383279502884197;
+  const int lane = threadIdx.x & 31;
+  const long long nwarp = (long long)gridDim.x * (blockDim.x >> 5);
+  for (long long cj = blockIdx.x * (long long)(blockDim.x >> 5) + (threadIdx.x >> 5);
+       cj < (long long)A.ncell * A.nrays; cj += nwarp) {
+    const int c = (int)(cj / A.nrays), j = (int)(cj % A.nrays);
+    // FRAC2 of escape_probability.F90:57 for this cell's temperature
+    const double frac2 = 1.0 / __dsqrt_rn(__dadd_rn(
+        __ddiv_rn(__ddiv_rn(__dmul_rn(8.0 * KB, A.T[c]), PI), MP), A.v2));
+    const int ne = A.epray[cj];
+    const long long p0 = A.offset[cj];
+    bool bad = (ne > 0) && (p0 < 0 || p0 + ne >= A.npoint);
+    // lines in chunks of 64, two per lane, so that each point's step length is
+    // computed once per chunk; a point's term g_u n_l - g_l n_u is shared by the
+    // two steps it ends and starts
+    for (int l0 = 0; l0 < A.nlin; l0 += 64) {
+      int u[2], d[2];
+      double gu[2], gd[2], f12[2], prev[2], tau[2];
+      bool act[2];
+#pragma unroll
+      for (int s = 0; s < 2; s++) {
+        const int l = l0 + 32 * s + lane;
+        act[s] = l < A.nlin;
+        u[s] = act[s] ? A.up[l] : 0;
+        d[s] = act[s] ? A.lo[l] : 0;
+        gu[s] = act[s] ? A.weights[u[s]] : 1.0;
+        gd[s] = act[s] ? A.weights[d[s]] : 1.0;
+        f12[s] = act[s] ? __dmul_rn(A.frac1[l], frac2) : 0.0;
+        tau[s] = 0.0;
+        prev[s] = 0.0;
+      }
+      bool badl = bad;
+      if (ne > 0 && !bad) {
+        const int ga = A.gp[p0];
+        if (ga < 0 || ga >= A.ngrid) badl = true;
+        else {
+          const double *pa = A.pop + (size_t)ga * A.nlev;
+#pragma unroll
+          for (int s = 0; s < 2; s++)
+            if (act[s]) prev[s] = __dsub_rn(__dmul_rn(pa[d[s]], gu[s]), __dmul_rn(pa[u[s]], gd[s]));
+        }
+        for (int i = 1; i <= ne && !badl; i++) {
+          const long long p = p0 + i;
+          const int gb = A.gp[p];
+          if (gb < 0 || gb >= A.ngrid) { badl = true; break; }
+          const double step = step_length(A.xyz, p);
+          const double *pb = A.pop + (size_t)gb * A.nlev;
+#pragma unroll
+          for (int s = 0; s < 2; s++)
+            if (act[s]) {
+              const double cur = __dsub_rn(__dmul_rn(pb[d[s]], gu[s]), __dmul_rn(pb[u[s]], gd[s]));
+              const double frac3 = __ddiv_rn(__dadd_rn(prev[s], cur) * 0.5, gd[s]);
+              tau[s] = __dadd_rn(tau[s], __dmul_rn(__dmul_rn(__dmul_rn(f12[s], frac3), step), PC));
+              prev[s] = cur;
+            }
+        }
+      }
+#pragma unroll
+      for (int s = 0; s < 2; s++)
+        if (act[s]) A.tau[((size_t)c * A.nlin + l0 + 32 * s + lane) * A.nrays + j] = badl ? nan("") : tau[s];
+    }
+  }
+}
+
 }  // namespace
+
+int launch_tau(const pdr_coolant *cool, const pdr_rays &r, const double *pop, const double *T, double v_turb,
+               double *tau, int sm_count, cudaStream_t st) {
+  TauArgs A;
+  A.ncell = r.ncell;
+  A.nrays = r.nrays;
+  A.ngrid = r.ngrid;
+  A.npoint = r.npoint;
+  A.nlev = cool->dev.nlev;
+  A.nlin = cool->dev.nlin;
+  A.epray = r.d_epray;
+  A.offset = r.d_offset;
+  A.xyz = r.d_xyz;
+  A.gp = r.d_gridpoint;
+  A.pop = pop;
+  A.T = T;
+  A.weights = cool->dev.weights;
+  A.frac1 = cool->dev.line_frac1;
+  A.up = cool->dev.line_up;
+  A.lo = cool->dev.line_lo;
+  A.v2 = v_turb * v_turb;
+  A.tau = tau;
+  const long long warps = (long long)r.ncell * r.nrays;
+  const int blocks = (int)std::max(1ll, std::min((warps + 3) / 4, (long long)sm_count * 16));
+  tau_kernel<<<blocks, 128, 0, st>>>(A);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? 0 : cuda_fail(e, "tau_kernel launch");
+}
 
 int launch_uvfield(const pdr_rays &r, const double *rho, int field, const double *G, const double *vectors,
                    double metallicity, double *colden, double *AV, double *rad, double *uv, int sm_count,

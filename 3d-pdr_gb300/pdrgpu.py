@@ -98,6 +98,7 @@ def lib():
     L.pdr_lte_batched.argtypes = [_vp, C.c_int] + [_vp] * 5
     L.pdr_uvfield_batched.argtypes = [C.POINTER(Rays), _vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                       C.c_double, _vp, _vp, _vp, _vp, _vp]
+    L.pdr_optical_depths_batched.argtypes = [_vp, C.POINTER(Rays), _vp, _vp, C.c_double, _vp, _vp]
     L.pdr_column_densities_batched.argtypes = [C.POINTER(Rays), _vp, _vp, C.c_int, C.POINTER(C.c_int), C.c_int,
                                                _vp, _vp]
     L.pdr_solver_create.argtypes = [_vp, C.c_int, C.POINTER(ChemOpts), C.POINTER(_vp)]
@@ -452,4 +453,13 @@ def column_densities(rays, rho, abundance, species=None, stream=None):
     out = torch.empty((rays.ncell, rays.nrays, nsel), dtype=torch.float64, device=rho.device)
     check(lib().pdr_column_densities_batched(C.byref(rays), _ptr(rho), _ptr(abundance), nspec, sp, nsel, _ptr(out),
                                              _stream(stream)), "pdr_column_densities_batched")
+    return out
+
+
+def optical_depths(cool, rays, pop, T, v_turb, stream=None):
+    """Line optical depths along the rays: (ncell, nlin, nrays), the layout level_populations takes."""
+    import torch
+    out = torch.empty((rays.ncell, cool.nlin, rays.nrays), dtype=torch.float64, device=pop.device)
+    check(lib().pdr_optical_depths_batched(cool.handle, C.byref(rays), _ptr(pop), _ptr(T), float(v_turb), _ptr(out),
+                                           _stream(stream)), "pdr_optical_depths_batched")
     return out

@@ -325,6 +325,15 @@ def ray_columns_grid(G, W, dev, stream, n=64, maxpoints=12):
         f()
         ms = _timed(f, stream, 5)
     npts = int(r["epray"].sum())
+    # the LVG step's optical depths of CO's 40 lines along the same rays, from
+    # LTE populations of every grid point at seeded temperatures
+    cool = G.Coolant("CO")
+    Tg = torch.as_tensor(W._rng(1009).uniform(10.0, 300.0, r["ngrid"]), device=dev)
+    pop, _ = G.lte_populations(cool, Tg, rho * W.COOLANT_X["CO"], stream=stream)
+    g = lambda: G.optical_depths(cool, rays, pop, Tg, 1.0e5, stream=stream)
+    with torch.cuda.stream(stream):
+        g()
+        ms_tau = _timed(g, stream, 5)
     # algorithmic bytes: per visited point (both passes) coordinates, grid index,
     # density and 5 abundances; per ray its count and offset; the outputs
     bytes_ = npts * (2 * (24 + 4 + 8) + 5 * 8) + r["ncell"] * 12 * (2 * 12 + 3 * 8 + 5 * 8) + r["ncell"] * 8
@@ -338,6 +347,8 @@ def ray_columns_grid(G, W, dev, stream, n=64, maxpoints=12):
     return {"workload": f"{n}^3 lattice, 12 rays, <= {maxpoints} evaluation points per ray "
                         f"({npts} points visited), 5 species columns + UV field",
             "ms": ms, "cells_per_s": r["ncell"] / (ms * 1e-3), "algorithmic_GBps": bytes_ / (ms * 1e-3) / 1e9,
+            "co_optical_depths": {"ms": ms_tau, "cells_per_s": r["ncell"] / (ms_tau * 1e-3),
+                                  "line_ray_sums_per_s": r["ncell"] * 12 * 40 / (ms_tau * 1e-3)},
             "cpu_baseline": {"cells_per_s": ncpu / cdt, "cores": os.cpu_count() or 1, "kind": "port",
                              "sample": f"first {ncpu} cells ({cdt:.2f} s)"}}
 
@@ -411,7 +422,7 @@ def main():
 
     # launch shape picked by the library's autotuner on a sample of this grid
     opts = {p: (G.chem_opts(p) if a.no_autotune else
-                G.autotune(net, ab0, rate, dens, G.chem_opts(p), ncell_sample=min(ncell, 8192), stream=stream))
+                G.autotune(net, ab0, rate, dens, G.chem_opts(p), ncell_sample=min(ncell, 32768), stream=stream))
             for p in ("mixed", "fp64")}
 
     def step(precision):

@@ -279,6 +279,16 @@ int pdr_uvfield_batched(const pdr_rays *rays, const double *d_rho, int field, co
 int pdr_column_densities_batched(const pdr_rays *rays, const double *d_rho, const double *d_abundance,
                                  int nspec, const int *species, int nsel, double *d_columns, void *stream);
 
+/* Optical depths of a coolant's radiative lines along the rays: the sums of
+ * escape_probability.F90:86-106 from the level populations of the grid points
+ * at the rays' evaluation points.  d_pop[ngrid*nlev] are the populations of
+ * every grid point (the gathers of 3DPDR.F90:736-751 read them), d_T[ncell]
+ * the cells' gas temperatures (Tguess), v_turb in cm/s.  Output
+ * d_tau[(c*nlin + l)*nrays + j] for line l in file order -- the layout
+ * pdr_levpop_batched takes.  A ray with a bad index gets NaN. */
+int pdr_optical_depths_batched(const pdr_coolant *c, const pdr_rays *rays, const double *d_pop, const double *d_T,
+                               double v_turb, double *d_tau, void *stream);
+
 /* ---- heating: batched CALC_HEATING (sub_calculate_heating.F90:7-386) ----
  * network 0 = reduced, 1 = full (the reference's compile-time choice of the
  * chemical-heating reactions); d_abundance[ncell*nspec] and d_rate[ncell*nreac]

@@ -102,6 +102,7 @@ def _load():
     lib.orc_uvfield.argtypes = [C.c_int, C.c_int, _ip, _lp64, _dp, _ip, _dp, C.c_int, _dp, _dp, C.c_double,
                                 _dp, _dp, _dp, _dp]
     lib.orc_columns.argtypes = [C.c_int, C.c_int, _ip, _lp64, _dp, _ip, _dp, _dp, C.c_int, _ip, C.c_int, _dp]
+    lib.orc_tau.argtypes = [C.POINTER(OrcCoolant), C.c_int, C.c_int, _ip, _lp64, _dp, _ip, _dp, _dp, C.c_double, _dp]
     return lib
 
 
@@ -237,6 +238,16 @@ class Coolant:
         self.col = np.ctypeslib.as_array(c.col, (7, nl, nl, self.ntemp)).copy()
         self.line_up = np.ctypeslib.as_array(c.line_up, (self.nlin,)).copy()
         self.line_lo = np.ctypeslib.as_array(c.line_lo, (self.nlin,)).copy()
+
+    def optical_depths(self, r, pop, T, v_turb):
+        """Line optical depths along the rays of workloads.rays(): (ncell, nlin, nrays)."""
+        ep, off, xyz, gp = _rays_arrays(r)
+        pop = np.ascontiguousarray(pop, dtype=np.float64)
+        T = np.ascontiguousarray(T, dtype=np.float64)
+        out = np.zeros(r["ncell"] * self.nlin * r["nrays"])
+        lib().orc_tau(self.p, r["ncell"], r["nrays"], _ptr(ep, _ip), off.ctypes.data_as(C.POINTER(C.c_longlong)),
+                      _ptr(xyz), _ptr(gp, _ip), _ptr(pop), _ptr(T), v_turb, _ptr(out))
+        return out.reshape(r["ncell"], self.nlin, r["nrays"])
 
     def lte(self, T, density):
         pop = np.zeros(self.nlev)

@@ -79,3 +79,35 @@ void orc_columns(int ncell, int nrays, const int *epray, const long long *offset
       }
     }
 }
+
+/* escape_probability.F90:57-106: the optical depth of every radiative line of
+ * a coolant along every ray, from the populations pop[gridpoint*nlev + level]
+ * of the grid points at the evaluation points; tau[(c*nlin + l)*nrays + j]. */
+void orc_tau(const orc_coolant *cl, int ncell, int nrays, const int *epray, const long long *offset, const double *xyz,
+             const int *gp, const double *pop, const double *T, double v_turb, double *tau) {
+  const double KB = 1.38065040e-16, MP = 1.67262164e-24, C = 2.99792458e+10;
+  const double PI = 3.141592653589793238462643383279502884197;
+  const int nlev = cl->nlev;
+#pragma omp parallel for schedule(static)
+  for (int c = 0; c < ncell; c++) {
+    const double frac2 = 1.0 / sqrt(8.0 * KB * T[c] / PI / MP + v_turb * v_turb);
+    for (int l = 0; l < cl->nlin; l++) {
+      const int il = cl->line_up[l], jl = cl->line_lo[l];
+      const double f = cl->freq[il * nlev + jl];
+      const double frac1 = (cl->A[il * nlev + jl] * (C * C * C)) / (8.0 * PI * (f * f * f));
+      const double wi = cl->weights[il], wj = cl->weights[jl];
+      for (int j = 0; j < nrays; j++) {
+        const long long cj = (long long)c * nrays + j;
+        double t = 0.0;
+        for (int i = 1; i <= epray[cj]; i++) {
+          const long long p = offset[cj] + i;
+          const double *pa = pop + (long long)gp[p - 1] * nlev, *pb = pop + (long long)gp[p] * nlev;
+          const double frac3 = ((pa[jl] * wi - pa[il] * wj) + (pb[jl] * wi - pb[il] * wj)) / 2. / wj;
+          const double rhs2 = step_length(xyz, p);
+          t = t + frac1 * frac2 * frac3 * rhs2 * PC_;
+        }
+        tau[((long long)c * cl->nlin + l) * nrays + j] = t;
+      }
+    }
+  }
+}

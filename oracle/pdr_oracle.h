@@ -171,6 +171,8 @@ void orc_uvfield(int ncell, int nrays, const int *epray, const long long *offset
                  double *colden, double *AV, double *rad, double *uv);
 void orc_columns(int ncell, int nrays, const int *epray, const long long *offset, const double *xyz, const int *gp,
                  const double *rho, const double *ab, int nspec, const int *species, int nsel, double *out);
+void orc_tau(const orc_coolant *cl, int ncell, int nrays, const int *epray, const long long *offset, const double *xyz,
+             const int *gp, const double *pop, const double *T, double v_turb, double *tau);
 
 /* whole per-cell level-population step for one coolant */
 int orc_levpop_batched(const orc_coolant *c, int ncell, const double *density, const double *T,

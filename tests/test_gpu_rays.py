@@ -57,3 +57,47 @@ def test_bad_grid_index_gives_nan_not_a_fault(cuda):
     o = out.cpu().numpy().reshape(-1, 3)
     assert np.isnan(o[ray]).all()
     assert np.isfinite(np.delete(o, ray, axis=0)).all()
+
+
+@pytest.mark.parametrize("key", ["CII", "CO"])
+def test_optical_depths_match_oracle(cuda, key):
+    """Line optical depths along the rays (escape_probability.F90:86-106), bit for bit."""
+    import torch
+    r = W.rays(6, 10)
+    oc = O.Coolant(key)
+    rng = np.random.Generator(np.random.PCG64(77))
+    dens = r["rho"] * W.COOLANT_X[key]
+    T = rng.uniform(10.0, 300.0, r["ngrid"])
+    pop = np.array([oc.lte(t, d) for t, d in zip(T, dens)]) * rng.uniform(0.5, 1.5, (r["ngrid"], oc.nlev))
+    ref = oc.optical_depths(r, pop, T[:r["ncell"]], 1.0e5)
+    rays, keep = G.device_rays(r, cuda)
+    out = G.optical_depths(G.Coolant(key), rays, torch.as_tensor(pop, device=cuda),
+                           torch.as_tensor(T[:r["ncell"]], device=cuda), 1.0e5)
+    torch.cuda.synchronize()
+    assert np.array_equal(out.cpu().numpy(), ref)
+
+
+def test_lvg_step_on_device_matches_oracle(cuda):
+    """tau from the neighbours' populations, then the level populations, all
+    on the device, against the same chain in the oracle (CO, pseudo-1D off)."""
+    import torch
+    key = "CO"
+    r = W.rays(5, 8)
+    oc = O.Coolant(key)
+    lp = W.levpop(ncell=r["ngrid"], seed=91)
+    dens = lp["n_H"] * W.COOLANT_X[key]
+    spop = np.array([oc.lte(t, d) for t, d in zip(lp["T"], dens)])
+    tau = oc.optical_depths(r, spop, lp["T"], 1.0e5)
+    pop_r, cool_r, _, _ = oc.levpop(lp["n_H"], lp["T"], lp["Td"], lp["partner5"], dens, spop, tau)
+    rays, keep = G.device_rays(r, cuda)
+    d = lambda a: torch.as_tensor(np.ascontiguousarray(a), device=cuda, dtype=torch.float64)
+    gc = G.Coolant(key)
+    gtau = G.optical_depths(gc, rays, d(spop), d(lp["T"]), 1.0e5)
+    pop, cool, _, status = G.level_populations(gc, d(lp["n_H"]), d(lp["T"]), d(lp["Td"]), d(lp["partner5"]),
+                                               d(dens), d(spop), gtau)
+    pop, cool = pop.cpu().numpy(), cool.cpu().numpy()
+    assert (status.cpu().numpy() == 0).all()
+    m = pop_r > 1e-6 * dens[:, None]
+    assert (np.abs(pop - pop_r)[m] / pop_r[m]).max() < 1e-6
+    mc = np.abs(cool_r) > 1e-40
+    assert (np.abs(cool - cool_r)[mc] / np.abs(cool_r[mc])).max() < 1e-6
