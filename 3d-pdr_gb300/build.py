@@ -16,7 +16,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 OUT = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "lib3dpdr_gb300.so")
-SOURCES = ["pdr_net.cpp", "coolant.cpp", "capi.cu", "chem_warp.cu", "chem_cta.cu", "chem_noalloc.cu", "rates.cu", "levpop.cu", "heating.cu", "probe.cu", "serve.cpp", "rays.cu"]
+SOURCES = ["pdr_net.cpp", "coolant.cpp", "capi.cu", "chem_warp.cu", "chem_cta.cu", "chem_noalloc.cu", "rates.cu", "levpop.cu", "heating.cu", "probe.cu", "serve.cpp", "rays.cu", "thermal.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
          "-Xcompiler", "-ffp-contract=off", f"-I{os.path.join(ROOT, 'include')}"]

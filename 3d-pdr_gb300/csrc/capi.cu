@@ -60,6 +60,13 @@ int launch_heating(const pdr_net *net, int network, const pdr_phys &ph, int ncel
                    const double *Tg, const double *Td, const double *uv, const double *ab, const double *rate,
                    double *out, cudaStream_t st);
 void shield_tables_host(double *xderiv30, double *scoderiv48);
+int launch_thermal(const pdr_thermal_params &p, int level_conv, int first_time, const double *heat, int hstride,
+                   int ncool, const double *const *cool, const pdr_thermal_state &s, double *total, int *nconv,
+                   cudaStream_t st);
+int launch_level_convergence(int ncell, int ncool, const int *nlev, const double *const *sol, double *const *pop,
+                             const double *ab, int nspec, const int *species, int thermal_balance,
+                             unsigned char *flags, unsigned char *cconv, int *counts, int sm_count,
+                             cudaStream_t st);
 
 static thread_local std::string g_err;
 
@@ -625,6 +632,56 @@ int pdr_heating_batched(const pdr_net *net, int network, const pdr_phys *phys, i
   if (ncell == 0) return 0;
   return launch_heating(net, network, *phys, ncell, d_density, d_Tgas, d_Tdust, d_uv_field, d_abundance, d_rate,
                         d_heating, (cudaStream_t)stream);
+}
+
+int pdr_thermal_balance_batched(const pdr_thermal_params *params, int level_conv, int first_time,
+                                const double *d_heating_total, int heating_stride, int ncool,
+                                const double *const *d_cooling, const pdr_thermal_state *state,
+                                double *d_total_cooling, int *d_nconverged, void *stream) {
+  bool ok = params && state && state->ncell >= 0 && heating_stride >= 1 && ncool >= 1 && ncool <= PDR_MAX_COOLANTS &&
+            d_cooling;
+  if (ok && state->ncell > 0) {
+    ok = d_heating_total && state->d_T && state->d_Tprev && state->d_Tlow && state->d_Thigh && state->d_Fmean &&
+         state->d_Fratio && state->d_flags;
+    for (int k = 0; ok && k < ncool; k++) ok = d_cooling[k] != nullptr;
+  }
+  if (!ok) {
+    set_error("pdr_thermal_balance_batched: invalid argument");
+    return PDR_E_ARG;
+  }
+  if (state->ncell == 0) {
+    if (d_nconverged) {
+      cudaError_t e = cudaMemsetAsync(d_nconverged, 0, sizeof(int), (cudaStream_t)stream);
+      if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(converged count)");
+    }
+    return 0;
+  }
+  return launch_thermal(*params, level_conv, first_time, d_heating_total, heating_stride, ncool, d_cooling, *state,
+                        d_total_cooling, d_nconverged, (cudaStream_t)stream);
+}
+
+int pdr_level_convergence_batched(int ncell, int ncool, const int *nlev, const double *const *d_solution,
+                                  double *const *d_pop, const double *d_abundance, int nspec, const int *species,
+                                  int thermal_balance, unsigned char *d_flags, unsigned char *d_coolant_conv,
+                                  int *d_counts, void *stream) {
+  bool ok = ncell >= 0 && ncool >= 1 && ncool <= PDR_MAX_COOLANTS && nlev && species && d_solution && d_pop &&
+            nspec > 0 && d_counts;
+  for (int k = 0; ok && k < ncool; k++)
+    ok = nlev[k] >= 1 && species[k] >= 0 && species[k] < nspec && (ncell == 0 || (d_solution[k] && d_pop[k]));
+  if (ok && ncell > 0) ok = d_abundance && d_flags;
+  if (!ok) {
+    set_error("pdr_level_convergence_batched: invalid argument");
+    return PDR_E_ARG;
+  }
+  if (ncell == 0) {
+    cudaError_t e = cudaMemsetAsync(d_counts, 0, sizeof(int) * (1 + ncool), (cudaStream_t)stream);
+    return e == cudaSuccess ? 0 : cuda_fail(e, "cudaMemsetAsync(level convergence counts)");
+  }
+  int dev = 0, sms = 0;
+  int rc = current_device(&dev, &sms);
+  if (rc) return rc;
+  return launch_level_convergence(ncell, ncool, nlev, d_solution, d_pop, d_abundance, nspec, species,
+                                  thermal_balance, d_flags, d_coolant_conv, d_counts, sms, (cudaStream_t)stream);
 }
 
 // diagnostic export of the shielding spline tables (tests compare them with the oracle)

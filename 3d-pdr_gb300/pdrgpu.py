@@ -53,6 +53,16 @@ class Phys(C.Structure):
                 ("h2form", C.c_int), ("xlambda_linear", C.c_int)]
 
 
+class ThermalParams(C.Structure):
+    _fields_ = [("Tmin", C.c_double), ("Tmax", C.c_double), ("Fcrit", C.c_double), ("Tdiff", C.c_double),
+                ("temp_fix", C.c_int)]
+
+
+class ThermalStateC(C.Structure):
+    _fields_ = [("ncell", C.c_int)] + [(k, _vp) for k in ("d_T", "d_Tprev", "d_Tlow", "d_Thigh", "d_Fmean",
+                                                            "d_Fratio", "d_flags")]
+
+
 def phys(zeta_s=5e-17, omega=0.42, grain_radius=1e-7, metallicity=1.0, g2d=100.0, v_turb_kms=1.0,
          h2form=1, xlambda_linear=0):
     """params.dat constants; zeta in s^-1 (stored as ZETA = zeta/1.3e-17)."""
@@ -101,6 +111,11 @@ def lib():
     L.pdr_optical_depths_batched.argtypes = [_vp, C.POINTER(Rays), _vp, _vp, C.c_double, _vp, _vp]
     L.pdr_column_densities_batched.argtypes = [C.POINTER(Rays), _vp, _vp, C.c_int, C.POINTER(C.c_int), C.c_int,
                                                _vp, _vp]
+    L.pdr_thermal_balance_batched.argtypes = [C.POINTER(ThermalParams), C.c_int, C.c_int, _vp, C.c_int, C.c_int,
+                                              C.POINTER(_vp), C.POINTER(ThermalStateC), _vp, _vp, _vp]
+    L.pdr_level_convergence_batched.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(_vp),
+                                                C.POINTER(_vp), _vp, C.c_int, C.POINTER(C.c_int), C.c_int, _vp, _vp,
+                                                _vp, _vp]
     L.pdr_solver_create.argtypes = [_vp, C.c_int, C.POINTER(ChemOpts), C.POINTER(_vp)]
     L.pdr_solver_run.argtypes = [_vp, C.c_int] + [_vp] * 7
     L.pdr_solver_free.argtypes = [_vp]
@@ -463,3 +478,109 @@ def optical_depths(cool, rays, pop, T, v_turb, stream=None):
     check(lib().pdr_optical_depths_batched(cool.handle, C.byref(rays), _ptr(pop), _ptr(T), float(v_turb), _ptr(out),
                                            _stream(stream)), "pdr_optical_depths_batched")
     return out
+
+
+# ---------------- outer-iteration controllers (3DPDR.F90:928-1229) ----------------
+
+TB_CONVERGED, TB_BINARY_CHOP, TB_LEVEL_TMIN, TB_LEVEL_CONVERGED, TB_HEATED, TB_COOLED = 1, 2, 4, 8, 16, 32
+
+
+class ThermalBalance:
+    """Per-cell thermal-balance state resident on the device (3DPDR.F90:928-1050).
+
+    T starts at Tguess with Tlow = Tlow0 and Thigh = Thigh0 (3DPDR.F90:282-288);
+    the defaults are params.dat's (Tmin 2.7 K, Tmax 30000 K, Fcrit 0.005,
+    Tdiff 0.01 K, TEMP_FIX on).  `flags` holds the PDR_TB_* bits."""
+
+    def __init__(self, T, Tlow0=10.0, Thigh0=8000.0, Tmin=2.7, Tmax=30000.0, Fcrit=0.005, Tdiff=0.01,
+                 temp_fix=True):
+        import torch
+        T = T.to(torch.float64).contiguous()
+        n = T.shape[0]
+        self.params = ThermalParams(Tmin, Tmax, Fcrit, Tdiff, 1 if temp_fix else 0)
+        self.T = T
+        self.Tprev = T.clone()
+        self.Tlow = torch.full_like(T, Tlow0)
+        self.Thigh = torch.full_like(T, Thigh0)
+        self.Fmean = torch.zeros_like(T)
+        self.Fratio = torch.zeros_like(T)
+        self.flags = torch.zeros(n, dtype=torch.uint8, device=T.device)
+        self.total_cooling = torch.zeros_like(T)
+        self.nconverged = torch.zeros(1, dtype=torch.int32, device=T.device)
+        self.level_counts = torch.zeros(1 + 8, dtype=torch.int32, device=T.device)
+        self.coolant_conv = torch.zeros(n, dtype=torch.uint8, device=T.device)
+
+    @property
+    def ncell(self):
+        return self.T.shape[0]
+
+    def _state(self):
+        return ThermalStateC(self.ncell, *[_ptr(t) for t in (self.T, self.Tprev, self.Tlow, self.Thigh, self.Fmean,
+                                                             self.Fratio, self.flags)])
+
+    def update(self, heating, cooling, level_conv, first_time, stream=None):
+        """One pass of the loop body: heating (ncell, 12) from `heating()` or the
+        (ncell,) totals; cooling the coolants' rates (CII, CI, OI, CO order).
+        Returns the device count of converged cells."""
+        if not heating.is_cuda or not heating.is_contiguous():
+            raise ValueError("expected a contiguous CUDA tensor")
+        hs = 12 if heating.dim() == 2 else 1
+        hp = _vp(heating.data_ptr() + (11 * 8 if hs == 12 else 0))
+        cl = (_vp * len(cooling))(*[_ptr(c) for c in cooling])
+        st = self._state()
+        check(lib().pdr_thermal_balance_batched(C.byref(self.params), int(bool(level_conv)), int(bool(first_time)),
+                                                hp, hs, len(cooling), cl, C.byref(st), _ptr(self.total_cooling),
+                                                _ptr(self.nconverged), _stream(stream)),
+              "pdr_thermal_balance_batched")
+        return self.nconverged
+
+    def level_convergence(self, solutions, pops, abundance, species, thermal_balance=True, stream=None):
+        """The RELCH check and population update of 3DPDR.F90:1084-1229; pops are
+        overwritten with solutions.  Returns the device counts [level-converged,
+        per coolant...]."""
+        k = len(solutions)
+        nlev = (C.c_int * k)(*[int(s.shape[1]) for s in solutions])
+        sp = (C.c_int * k)(*[int(x) for x in species])
+        sol = (_vp * k)(*[_ptr(s) for s in solutions])
+        pp = (_vp * k)(*[_ptr(p) for p in pops])
+        check(lib().pdr_level_convergence_batched(self.ncell, k, nlev, sol, pp, _ptr(abundance), abundance.shape[1],
+                                                  sp, int(bool(thermal_balance)), _ptr(self.flags),
+                                                  _ptr(self.coolant_conv), _ptr(self.level_counts), _stream(stream)),
+              "pdr_level_convergence_batched")
+        return self.level_counts[:1 + k]
+
+
+class OuterIteration:
+    """The driver's convergence bookkeeping between outer iterations
+    (3DPDR.F90:1064-1174), on host counts: `level_conv` enables the
+    thermal-balance update once the level populations have converged,
+    `first_time` selects its first bracket."""
+
+    def __init__(self, ncell, thermal_balance=True):
+        self.ncell = ncell
+        self.thermal_balance = thermal_balance
+        self.level_conv = False
+        self.first_time = True
+        self.done = False
+        self.reason = None
+
+    def after_thermal(self, nconverged):
+        """3DPDR.F90:1064-1082.  Returns True when every cell converged."""
+        if not self.thermal_balance:
+            return False
+        if self.level_conv and self.first_time:
+            self.first_time = False
+        if self.level_conv:
+            self.level_conv = False
+        if int(nconverged) == self.ncell:
+            self.done, self.reason = True, "thermal balance"
+        return self.done
+
+    def after_levels(self, level_converged):
+        """3DPDR.F90:1157-1174 on the count of level-converged cells."""
+        if int(level_converged) == self.ncell:
+            if self.thermal_balance:
+                self.level_conv = True
+            else:
+                self.done, self.reason = True, "level populations"
+        return self.done

@@ -353,6 +353,56 @@ def ray_columns_grid(G, W, dev, stream, n=64, maxpoints=12):
                              "sample": f"first {ncpu} cells ({cdt:.2f} s)"}}
 
 
+def thermal_controllers(G, W, dev, stream, n=1 << 21, n_lev=1 << 20):
+    """The outer-iteration controllers resident on the device: one
+    thermal-balance pass (3DPDR.F90:928-1050, the first-bracket branch, which
+    every unconverged cell takes) over 2^21 cells, and the level-population
+    convergence check plus population update (3DPDR.F90:1084-1229) for CII, CI,
+    OI and CO (5, 5, 5, 41 levels) over 2^20 cells."""
+    import torch
+    import oracle as O
+    rng = W._rng(1010)
+    T = rng.uniform(10.0, 3000.0, n)
+    heat = 10.0 ** rng.uniform(-24, -20, n)
+    cool = [heat * rng.uniform(0.1, 0.5, n) for _ in range(4)]
+    tb = G.ThermalBalance(torch.as_tensor(T, device=dev))
+    dh = torch.as_tensor(heat, device=dev)
+    dc = [torch.as_tensor(c, device=dev) for c in cool]
+    f = lambda: tb.update(dh, dc, 1, 1, stream=stream)
+    with torch.cuda.stream(stream):
+        f()
+        ms_t = _timed(f, stream, 20)
+    nlev = (5, 5, 5, 41)
+    sols = [torch.as_tensor(10.0 ** rng.uniform(-10, 0, (n_lev, m)), device=dev) for m in nlev]
+    pops = [s * 1.001 for s in sols]
+    ab = torch.as_tensor(10.0 ** rng.uniform(-8, -3, (n_lev, 33)), device=dev)
+    lc = G.ThermalBalance(torch.zeros(n_lev, dtype=torch.float64, device=dev))
+    g = lambda: lc.level_convergence(sols, pops, ab, (0, 5, 12, 20), stream=stream)
+    with torch.cuda.stream(stream):
+        g()
+        ms_l = _timed(g, stream, 20)
+    # algorithmic bytes per cell: thermal reads heating, 4 coolings, T and the
+    # flags and writes the cooling total, Fmean, Fratio, T, Tprev, one bound and
+    # the flags; the level check reads SOLUTION and the populations, writes the
+    # populations, reads 4 abundances and the flags and writes the flags and bits
+    b_t = (8 + 32 + 8 + 1) + (6 * 8 + 1)
+    b_l = sum(nlev) * 24 + 4 * 8 + 3
+    st = dict(T=T[: 1 << 18].copy(), Tprev=T[: 1 << 18].copy(), Tlow=np.full(1 << 18, 10.0),
+              Thigh=np.full(1 << 18, 8000.0), Fmean=np.zeros(1 << 18), Fratio=np.zeros(1 << 18),
+              flags=np.zeros(1 << 18, np.uint8))
+    t0 = time.perf_counter()
+    O.thermal_balance(st, heat[: 1 << 18], [c[: 1 << 18] for c in cool], 1, 1)
+    cdt = time.perf_counter() - t0
+    return {"workload": f"thermal-balance pass over {n} cells; level convergence of 4 coolants (5,5,5,41 levels) "
+                        f"over {n_lev} cells",
+            "thermal_ms": ms_t, "thermal_cells_per_s": n / (ms_t * 1e-3),
+            "thermal_algorithmic_GBps": n * b_t / (ms_t * 1e-3) / 1e9,
+            "level_check_ms": ms_l, "level_check_cells_per_s": n_lev / (ms_l * 1e-3),
+            "level_check_algorithmic_GBps": n_lev * b_l / (ms_l * 1e-3) / 1e9,
+            "cpu_baseline": {"thermal_cells_per_s": (1 << 18) / cdt, "cores": 1, "kind": "port",
+                             "sample": f"first {1 << 18} cells, oracle thermal pass ({cdt * 1e3:.1f} ms)"}}
+
+
 def run_reference(a, rank):
     if rank != 0:
         return
@@ -545,7 +595,8 @@ def main():
             extras["secondary"] = {"C2": full_network_sample(G, W, dev, stream),
                                    "C4": level_population_grid(G, W, dev, stream),
                                    "C5": served_stream(G, W),
-                                   "rays": ray_columns_grid(G, W, dev, stream)}
+                                   "rays": ray_columns_grid(G, W, dev, stream),
+                                   "thermal": thermal_controllers(G, W, dev, stream)}
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "cell-solves/s", "n_gpus": world, "steps": a.steps,
                 "warmup": a.warmup, "ms_per_step": ms_total / a.steps, "higher_is_better": True,

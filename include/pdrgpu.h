@@ -301,6 +301,64 @@ int pdr_heating_batched(const pdr_net *net, int network, const pdr_phys *phys, i
                         const double *d_uv_field, const double *d_abundance, const double *d_rate,
                         double *d_heating, void *stream);
 
+/* ---- outer-iteration controllers resident on the device ----
+ * The per-cell state of the thermal-balance search (3DPDR.F90:928-1050) lives
+ * in device memory between outer iterations.  d_flags bits: */
+#define PDR_TB_CONVERGED 1       /* converged(pp) */
+#define PDR_TB_BINARY_CHOP 2     /* dobinarychop(pp) */
+#define PDR_TB_LEVEL_TMIN 4      /* doleveltmin(pp) */
+#define PDR_TB_LEVEL_CONVERGED 8 /* level_converged(pp) */
+#define PDR_TB_HEATED 16         /* previouschange(pp) == "H" */
+#define PDR_TB_COOLED 32         /* previouschange(pp) == "C" (neither: not yet set) */
+#define PDR_MAX_COOLANTS 8
+
+typedef struct {
+  double Tmin, Tmax, Fcrit, Tdiff; /* params.dat thermal-balance block (input_parameters.F90:48-51) */
+  int temp_fix;                    /* the TEMP_FIX build option (on in the reference makefile) */
+} pdr_thermal_params;
+
+typedef struct {
+  int ncell;
+  double *d_T;     /* gastemperature, updated in place */
+  double *d_Tprev; /* previousgastemperature */
+  double *d_Tlow, *d_Thigh;
+  double *d_Fmean, *d_Fratio; /* written for the cells not yet converged */
+  unsigned char *d_flags;
+} pdr_thermal_state;
+
+/* One pass of the thermal-balance loop body (3DPDR.F90:928-1050) for every
+ * cell not yet converged: Fmean = heating - cooling, Fratio = 2|Fmean|/|heating
+ * + cooling|, then the first 30% bracket (level_conv && first_time), or the
+ * 30% steps, binary chop, TEMP_FIX and Tmin/Tmax ends (level_conv && !first_time);
+ * with level_conv == 0 only Fmean and Fratio are updated.  The heating of cell
+ * c is d_heating_total[c*heating_stride] (pass d_heating + 11, stride 12, for
+ * pdr_heating_batched's output); the cooling is the left-to-right sum of the
+ * ncool (<= PDR_MAX_COOLANTS) coolant rates, host array of device pointers
+ * d_cooling[k][ncell] (3DPDR.F90:897: CII, CI, OI, CO), stored in
+ * d_total_cooling (or NULL).  *d_nconverged (or NULL) receives the number of
+ * converged cells after the pass (3DPDR.F90:1067-1069). */
+int pdr_thermal_balance_batched(const pdr_thermal_params *params, int level_conv, int first_time,
+                                const double *d_heating_total, int heating_stride, int ncool,
+                                const double *const *d_cooling, const pdr_thermal_state *state,
+                                double *d_total_cooling, int *d_nconverged, void *stream);
+
+/* The level-population convergence check and update of 3DPDR.F90:1084-1229
+ * for ncool (<= PDR_MAX_COOLANTS) coolants: host arrays nlev[k], species[k]
+ * (the coolant's species, NCx NC NO NCO) and of device pointers
+ * d_solution[k][ncell*nlev[k]] (the new populations) and d_pop[k] (the
+ * current ones, overwritten with the new).  A level is checked when its new
+ * population is >= 1e-10 * abundance(species); the coolant converged in a cell
+ * when every checked level changed by a relative 2|s-p|/(s+p) <= 1e-2.  Sets
+ * PDR_TB_LEVEL_CONVERGED in d_flags where all coolants converged; with
+ * thermal_balance != 0 clears it everywhere once every cell converged
+ * (3DPDR.F90:1202-1206).  d_coolant_conv[ncell] (or NULL): bit k = coolant k
+ * converged.  d_counts[1+ncool]: level-converged cells before that reset, then
+ * the converged cells of each coolant. */
+int pdr_level_convergence_batched(int ncell, int ncool, const int *nlev, const double *const *d_solution,
+                                  double *const *d_pop, const double *d_abundance, int nspec, const int *species,
+                                  int thermal_balance, unsigned char *d_flags, unsigned char *d_coolant_conv,
+                                  int *d_counts, void *stream);
+
 /* ---- diagnostics (tests pin the device code against the reference with these) ----
  * The device network RHS, as the generated f() of odes_<net>.c:26-149 computes
  * it (mode 0: d_out[nstate*neq], x_e of each state in d_xe), or the analytic

@@ -103,6 +103,12 @@ def _load():
                                 _dp, _dp, _dp, _dp]
     lib.orc_columns.argtypes = [C.c_int, C.c_int, _ip, _lp64, _dp, _ip, _dp, _dp, C.c_int, _ip, C.c_int, _dp]
     lib.orc_tau.argtypes = [C.POINTER(OrcCoolant), C.c_int, C.c_int, _ip, _lp64, _dp, _ip, _dp, _dp, C.c_double, _dp]
+    _ucp = C.POINTER(C.c_ubyte)
+    lib.orc_thermal_balance.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int,
+                                        C.c_int, _dp, C.c_int, C.c_int, C.POINTER(_dp), _dp, _dp, _dp, _dp, _dp,
+                                        _dp, _dp, _ucp, _lp64]
+    lib.orc_level_convergence.argtypes = [C.c_int, C.c_int, _ip, C.POINTER(_dp), C.POINTER(_dp), _dp, C.c_int, _ip,
+                                          C.c_int, _ucp, _ucp, _lp64]
     return lib
 
 
@@ -326,3 +332,44 @@ def columns(r, species=None):
     lib().orc_columns(n, nr, _ptr(ep, _ip), off.ctypes.data_as(C.POINTER(C.c_longlong)), _ptr(xyz), _ptr(gp, _ip),
                       _ptr(rho), _ptr(ab), nspec, _ptr(sp, _ip) if sp is not None else None, nsel, _ptr(out))
     return out.reshape(n, nr, nsel)
+
+
+def thermal_balance(state, heating_total, cooling, level_conv, first_time, Tmin=2.7, Tmax=30000.0, Fcrit=0.005,
+                    Tdiff=0.01, temp_fix=True):
+    """3DPDR.F90:928-1050 on numpy state (dict of T, Tprev, Tlow, Thigh, Fmean,
+    Fratio float64 arrays and flags uint8), updated in place; returns
+    (total cooling, number converged)."""
+    n = state["T"].shape[0]
+    heat = np.ascontiguousarray(heating_total, dtype=np.float64)
+    cools = [np.ascontiguousarray(c, dtype=np.float64) for c in cooling]
+    cp = (_dp * len(cools))(*[_ptr(c) for c in cools])
+    for k in ("T", "Tprev", "Tlow", "Thigh", "Fmean", "Fratio"):
+        assert state[k].dtype == np.float64 and state[k].flags.c_contiguous
+    assert state["flags"].dtype == np.uint8
+    total = np.zeros(n)
+    nconv = C.c_longlong(0)
+    lib().orc_thermal_balance(n, Tmin, Tmax, Fcrit, Tdiff, 1 if temp_fix else 0, int(bool(level_conv)),
+                              int(bool(first_time)), _ptr(heat), 1, len(cools), cp,
+                              *[_ptr(state[k]) for k in ("T", "Tprev", "Tlow", "Thigh", "Fmean", "Fratio")],
+                              _ptr(total), state["flags"].ctypes.data_as(C.POINTER(C.c_ubyte)), C.byref(nconv))
+    return total, nconv.value
+
+
+def level_convergence(solutions, pops, abundance, species, flags, thermal_balance=True):
+    """3DPDR.F90:1084-1229: pops (list of (ncell, nlev) float64) overwritten with
+    solutions, flags updated; returns (coolant_conv bits, counts)."""
+    k = len(solutions)
+    n = solutions[0].shape[0]
+    sols = [np.ascontiguousarray(s, dtype=np.float64) for s in solutions]
+    for p in pops:
+        assert p.dtype == np.float64 and p.flags.c_contiguous
+    ab = np.ascontiguousarray(abundance, dtype=np.float64)
+    nlev = (C.c_int * k)(*[s.shape[1] for s in sols])
+    sp = (C.c_int * k)(*[int(x) for x in species])
+    cconv = np.zeros(n, dtype=np.uint8)
+    counts = np.zeros(1 + k, dtype=np.int64)
+    lib().orc_level_convergence(n, k, nlev, (_dp * k)(*[_ptr(s) for s in sols]), (_dp * k)(*[_ptr(p) for p in pops]),
+                                _ptr(ab), ab.shape[1], sp, int(bool(thermal_balance)),
+                                flags.ctypes.data_as(C.POINTER(C.c_ubyte)), cconv.ctypes.data_as(C.POINTER(C.c_ubyte)),
+                                counts.ctypes.data_as(C.POINTER(C.c_longlong)))
+    return cconv, counts

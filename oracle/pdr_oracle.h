@@ -188,6 +188,17 @@ void orc_heating(const orc_net *net, int network, const orc_phys *ph, double den
                  double Tg, double Td, double uv_field, const double *abundance,
                  const double *rate, const int *nr, double *heating12);
 
+/* ---------------- thermal balance (3DPDR.F90:928-1050, 1084-1229) ---------------- */
+void orc_thermal_balance(int ncell, double Tmin, double Tmax, double Fcrit, double Tdiff, int temp_fix,
+                         int level_conv, int first_time, const double *heating, int hstride, int ncool,
+                         const double *const *cooling, double *T, double *Tprev, double *Tlow, double *Thigh,
+                         double *Fmean, double *Fratio, double *total_cooling, unsigned char *flags,
+                         long long *nconverged);
+void orc_level_convergence(int ncell, int ncool, const int *nlev, const double *const *solution,
+                           double *const *pop, const double *abundance, int nspec, const int *species,
+                           int thermal_balance, unsigned char *flags, unsigned char *coolant_conv,
+                           long long *counts);
+
 #ifdef __cplusplus
 }
 #endif
