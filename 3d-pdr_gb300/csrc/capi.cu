@@ -667,7 +667,7 @@ int pdr_level_convergence_batched(int ncell, int ncool, const int *nlev, const d
   bool ok = ncell >= 0 && ncool >= 1 && ncool <= PDR_MAX_COOLANTS && nlev && species && d_solution && d_pop &&
             nspec > 0 && d_counts;
   for (int k = 0; ok && k < ncool; k++)
-    ok = nlev[k] >= 1 && species[k] >= 0 && species[k] < nspec && (ncell == 0 || (d_solution[k] && d_pop[k]));
+    ok = nlev[k] >= 1 && nlev[k] <= 4096 && species[k] >= 0 && species[k] < nspec && (ncell == 0 || (d_solution[k] && d_pop[k]));
   if (ok && ncell > 0) ok = d_abundance && d_flags;
   if (!ok) {
     set_error("pdr_level_convergence_batched: invalid argument");

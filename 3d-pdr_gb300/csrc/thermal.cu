@@ -7,8 +7,11 @@
 // reads back only the counts it prints (converged cells, level-converged
 // cells per coolant).  The arithmetic is the reference's: the cooling total is
 // the left-to-right sum of the coolants (3DPDR.F90:897), the 30% brackets are
-// 1.3D0*T and 0.7D0*T, the binary chop (a+b)/2.0D0 -- no products feed an add,
-// so nothing is contracted and the results are bit-identical to the host's.
+// 1.3D0*T and 0.7D0*T, the binary chop (a+b)/2.0D0 (taken as (a+b)*0.5, the
+// same correctly rounded value) -- no products feed an add, so nothing is
+// contracted and the results are bit-identical to the host's.
+#include <cstdint>
+
 #include "pdr_internal.h"
 
 namespace pdr {
@@ -86,21 +89,21 @@ __global__ void __launch_bounds__(256) thermal_kernel(const __grid_constant__ Th
             if (t < A.Tmin) t = tlow = thigh = A.Tmin;
           }
           if (fm > 0.0 && (f & COOL)) {
-            t = __ddiv_rn(__dadd_rn(thigh, tlow), 2.0);
+            t = __dmul_rn(__dadd_rn(thigh, tlow), 0.5);
             f |= CHOP;
           }
           if (fm < 0.0 && (f & HEAT)) {
-            t = __ddiv_rn(__dadd_rn(thigh, tlow), 2.0);
+            t = __dmul_rn(__dadd_rn(thigh, tlow), 0.5);
             f |= CHOP;
           }
         } else {
           if (fm > 0.0) {
             tlow = t;
-            t = __ddiv_rn(__dadd_rn(t, thigh), 2.0);
+            t = __dmul_rn(__dadd_rn(t, thigh), 0.5);
           }
           if (fm < 0.0) {
             thigh = t;
-            t = __ddiv_rn(__dadd_rn(t, tlow), 2.0);
+            t = __dmul_rn(__dadd_rn(t, tlow), 0.5);
           }
         }
         // TEMP_FIX (3DPDR.F90:1007-1022), then the Tmin/Tmax ends (:1025-1048)
@@ -132,8 +135,9 @@ __global__ void __launch_bounds__(256) thermal_kernel(const __grid_constant__ Th
 }
 
 struct LevConvArgs {
-  int ncell, ncool, nspec;
+  int ncell, ncool, nspec, vec;
   int nlev[PDR_MAX_COOLANTS], species[PDR_MAX_COOLANTS];
+  float inv_nlev[PDR_MAX_COOLANTS];
   const double *sol[PDR_MAX_COOLANTS];
   double *pop[PDR_MAX_COOLANTS];
   const double *ab;
@@ -142,51 +146,125 @@ struct LevConvArgs {
 };
 
 constexpr int LC_CELLS = 256;   // cells per block; one thread per cell for the flags
+constexpr int LC_BATCH = 4;     // element pairs in flight per thread
 
-// Each block owns LC_CELLS consecutive cells.  Its threads sweep the
-// coolants' [cell][level] arrays over that range with coalesced element
-// strides, mark a cell's coolant unconverged in shared memory (an idempotent
-// store), and copy SOLUTION into the populations; then one thread per cell
-// combines the marks into the flags and the counts.
+// One level's check (3DPDR.F90:1090-1102): returns true when the level is
+// checked and changed by more than 1e-2, i.e. sv >= floor and
+// 2|(sv-pv)/(sv+pv)| > 1e-2, in the reference's FP64 operations.
+__device__ __forceinline__ bool level_moved_fp64(double sv, double pv, double floor) {
+  if (!(sv >= floor)) return false;
+  double relch = 0.0;
+  if (!(sv == 0.0 && pv == 0.0)) relch = __dmul_rn(2.0, fabs(__ddiv_rn(__dsub_rn(sv, pv), __dadd_rn(sv, pv))));
+  return relch > 1.0e-2;
+}
+
+// The same decision, settled in integer arithmetic where that is certain.
+// For positive normal finite doubles the bit pattern read as an integer, over
+// 2^52, is L(x) = E + f for x = 2^(E-1023) (1+f), a continuous monotone map
+// whose slope against ln x lies in [1, 2): |ln s - ln p| is between
+// |dL|/2 and |dL|.  The relative change 2|s-p|/(s+p) = 2 tanh(|ln s - ln p|/2)
+// exceeds 1e-2 exactly when |ln s - ln p| > 0.01000008, so |dL| <= 0.0099
+// means "not moved" and |dL| >= 0.0202 means "moved", with margins far beyond
+// the FP64 rounding of the reference's expression.  Everything else -- the
+// band between, zeros, negatives, subnormals, infinities, NaN -- takes the
+// FP64 path.  Positive s passes s >= floor exactly when its bits are >= the
+// floor's for floor > 0, always for floor <= 0, never for a NaN floor.
+__device__ __forceinline__ bool level_moved(double sv, double pv, double floor) {
+  constexpr unsigned long long MIN_NORMAL = 0x0010000000000000ull, INF = 0x7FF0000000000000ull;
+  constexpr long long NOT_MOVED = 44585636310967ll;   // floor(0.0099 * 2^52)
+  constexpr long long MOVED = 90972712472885ll;       // ceil(0.0202 * 2^52)
+  const unsigned long long sb = __double_as_longlong(sv), pb = __double_as_longlong(pv);
+  if (sb - MIN_NORMAL < INF - MIN_NORMAL && pb - MIN_NORMAL < INF - MIN_NORMAL) {
+    const unsigned long long fb = __double_as_longlong(floor);
+    const unsigned long long fkey =
+        (fb & 0x7FFFFFFFFFFFFFFFull) > INF ? ~0ull : ((fb >> 63) ? 0ull : fb);
+    if (sb < fkey) return false;
+    const long long d = (long long)sb - (long long)pb;
+    const long long ad = d < 0 ? -d : d;
+    if (ad <= NOT_MOVED) return false;
+    if (ad >= MOVED) return true;
+  }
+  return level_moved_fp64(sv, pv, floor);
+}
+
+// Each block owns LC_CELLS consecutive cells.  The per-cell floors
+// 1e-10 * abundance(species) go to shared memory first; then the threads sweep
+// each coolant's [cell][level] arrays over the block's range in 16-byte pairs
+// (LC_BATCH pairs loaded before any is used), mark a cell's coolant
+// unconverged in shared memory (an idempotent store) and copy SOLUTION into the
+// populations; finally one thread per cell combines the marks into the flags
+// and the counts.  The cell of element e is floor((e + 0.5) / nlev), taken in
+// FP32: e < LC_CELLS * nlev keeps it exact.
 __global__ void __launch_bounds__(LC_CELLS) levconv_kernel(const __grid_constant__ LevConvArgs A) {
   __shared__ unsigned char bad[PDR_MAX_COOLANTS][LC_CELLS];
+  __shared__ double floor_of[PDR_MAX_COOLANTS][LC_CELLS];
   const int c0 = blockIdx.x * LC_CELLS;
   const int ncb = min(LC_CELLS, A.ncell - c0);
-  for (int k = 0; k < A.ncool; k++) bad[k][threadIdx.x] = 0;
+  const int t = threadIdx.x;
+  for (int k = 0; k < A.ncool; k++) {
+    bad[k][t] = 0;
+    if (t < ncb) floor_of[k][t] = __dmul_rn(A.ab[(size_t)(c0 + t) * A.nspec + A.species[k]], 1.0e-10);
+  }
   __syncthreads();
   for (int k = 0; k < A.ncool; k++) {
     const int n = A.nlev[k];
+    const float inv = A.inv_nlev[k];
     const size_t base = (size_t)c0 * n;
     const int ne = ncb * n;
     const double *s = A.sol[k] + base;
     double *p = A.pop[k] + base;
-    for (int e = threadIdx.x; e < ne; e += LC_CELLS) {
-      const int cl = e / n;
-      const double sv = s[e], pv = p[e];
-      const double floor = __dmul_rn(A.ab[(size_t)(c0 + cl) * A.nspec + A.species[k]], 1.0e-10);
-      if (sv >= floor) {
-        double relch = 0.0;
-        if (!(sv == 0.0 && pv == 0.0))
-          relch = __dmul_rn(2.0, fabs(__ddiv_rn(__dsub_rn(sv, pv), __dadd_rn(sv, pv))));
-        if (relch > 1.0e-2) bad[k][cl] = 1;
+    int e0 = 0;
+    if (A.vec) {
+      // base is a multiple of LC_CELLS elements and the arrays are 16-byte aligned
+      const int npair = ne >> 1;
+      const double2 *s2 = reinterpret_cast<const double2 *>(s);
+      double2 *p2 = reinterpret_cast<double2 *>(p);
+      for (int q0 = t; q0 < npair; q0 += LC_CELLS * LC_BATCH) {
+        double2 sv[LC_BATCH], pv[LC_BATCH];
+#pragma unroll
+        for (int u = 0; u < LC_BATCH; u++) {
+          const int q = q0 + u * LC_CELLS;
+          if (q < npair) {
+            sv[u] = s2[q];
+            pv[u] = p2[q];
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < LC_BATCH; u++) {
+          const int q = q0 + u * LC_CELLS;
+          if (q < npair) {
+            const int ea = 2 * q, eb = ea + 1;
+            const int ca = __float2int_rz(__fmul_rn(__int2float_rn(ea) + 0.5f, inv));
+            const int cb = __float2int_rz(__fmul_rn(__int2float_rn(eb) + 0.5f, inv));
+            if (level_moved(sv[u].x, pv[u].x, floor_of[k][ca])) bad[k][ca] = 1;
+            if (level_moved(sv[u].y, pv[u].y, floor_of[k][cb])) bad[k][cb] = 1;
+            p2[q] = sv[u];   // 3DPDR.F90:1212-1229
+          }
+        }
       }
-      p[e] = sv;   // 3DPDR.F90:1212-1229
+      e0 = npair * 2;
+    }
+    for (int e = e0 + t; e < ne; e += LC_CELLS) {
+      const int cl = __float2int_rz(__fmul_rn(__int2float_rn(e) + 0.5f, inv));
+      const double sv = s[e];
+      if (level_moved(sv, p[e], floor_of[k][cl])) bad[k][cl] = 1;
+      p[e] = sv;
     }
   }
   __syncthreads();
-  const int c = c0 + threadIdx.x;
-  const bool live = threadIdx.x < ncb;
+  const int c = c0 + t;
+  const bool live = t < ncb;
+  const unsigned all_mask = (1u << A.ncool) - 1u;
   unsigned conv = 0;
   if (live) {
     for (int k = 0; k < A.ncool; k++)
-      if (!bad[k][threadIdx.x]) conv |= 1u << k;
-    const bool all = conv == (1u << A.ncool) - 1u;
+      if (!bad[k][t]) conv |= 1u << k;
     unsigned f = A.flags[c] & ~LCONV;
-    if (all) f |= LCONV;
+    if (conv == all_mask) f |= LCONV;
     A.flags[c] = (unsigned char)f;
     if (A.cconv) A.cconv[c] = (unsigned char)conv;
   }
-  count_add(&A.counts[0], live && conv == (1u << A.ncool) - 1u);
+  count_add(&A.counts[0], live && conv == all_mask);
   for (int k = 0; k < A.ncool; k++) count_add(&A.counts[1 + k], live && ((conv >> k) & 1u));
 }
 
@@ -241,11 +319,14 @@ int launch_level_convergence(int ncell, int ncool, const int *nlev, const double
   A.ncell = ncell;
   A.ncool = ncool;
   A.nspec = nspec;
+  A.vec = 1;
   for (int k = 0; k < ncool; k++) {
     A.nlev[k] = nlev[k];
+    A.inv_nlev[k] = 1.0f / (float)nlev[k];
     A.species[k] = species[k];
     A.sol[k] = sol[k];
     A.pop[k] = pop[k];
+    if ((reinterpret_cast<uintptr_t>(sol[k]) | reinterpret_cast<uintptr_t>(pop[k])) & 15) A.vec = 0;
   }
   A.ab = ab;
   A.flags = flags;

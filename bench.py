@@ -353,10 +353,10 @@ def ray_columns_grid(G, W, dev, stream, n=64, maxpoints=12):
                              "sample": f"first {ncpu} cells ({cdt:.2f} s)"}}
 
 
-def thermal_controllers(G, W, dev, stream, n=1 << 21, n_lev=1 << 20):
+def thermal_controllers(G, W, dev, stream, n=1 << 23, n_lev=1 << 20):
     """The outer-iteration controllers resident on the device: one
     thermal-balance pass (3DPDR.F90:928-1050, the first-bracket branch, which
-    every unconverged cell takes) over 2^21 cells, and the level-population
+    every unconverged cell takes) over 2^23 cells, and the level-population
     convergence check plus population update (3DPDR.F90:1084-1229) for CII, CI,
     OI and CO (5, 5, 5, 41 levels) over 2^20 cells."""
     import torch

@@ -344,7 +344,7 @@ int pdr_thermal_balance_batched(const pdr_thermal_params *params, int level_conv
 
 /* The level-population convergence check and update of 3DPDR.F90:1084-1229
  * for ncool (<= PDR_MAX_COOLANTS) coolants: host arrays nlev[k], species[k]
- * (the coolant's species, NCx NC NO NCO) and of device pointers
+ * (the coolant's species, NCx NC NO NCO; nlev <= 4096) and of device pointers
  * d_solution[k][ncell*nlev[k]] (the new populations) and d_pop[k] (the
  * current ones, overwritten with the new).  A level is checked when its new
  * population is >= 1e-10 * abundance(species); the coolant converged in a cell
