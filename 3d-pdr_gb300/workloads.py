@@ -160,3 +160,27 @@ def rays(n=8, maxpoints=12, spacing_pc=0.05, step_pc=0.05, nspec=33, seed=1007):
     return dict(ncell=ncell, nrays=nrays, ngrid=ncell, npoint=ncell * nrays * (maxpoints + 1),
                 epray=epray.reshape(-1), offset=offset, xyz=xyz.reshape(-1, 3), gridpoint=gp.reshape(-1),
                 rho=rho, abundance=ab, vectors=d)
+
+
+def slab_rays(x, ray=6):
+    """Evaluation points of a PSEUDO_1D slab (points at x[i] pc on the x axis,
+    illuminated on the x = 0 face): HEALPix ray `ray` (6 = -x) of every cell
+    runs from the cell through every point nearer the face, in order; the
+    other rays carry no points.  Same dict layout as rays()."""
+    x = np.asarray(x, dtype=np.float64)
+    n = len(x)
+    nrays = 12
+    order = np.argsort(-x, kind="stable")
+    epray = np.zeros((n, nrays), np.int32)
+    offset = np.zeros((n, nrays), np.int64)
+    gp = []
+    for c in range(n):
+        pts = [c] + [int(j) for j in order if x[j] < x[c]]
+        offset[c, :] = len(gp)
+        epray[c, ray] = len(pts) - 1
+        gp += pts
+    gp = np.array(gp, np.int32)
+    xyz = np.zeros((len(gp), 3))
+    xyz[:, 0] = x[gp]
+    return dict(ncell=n, nrays=nrays, ngrid=n, npoint=len(gp), epray=epray.reshape(-1), offset=offset.reshape(-1),
+                xyz=xyz, gridpoint=gp, vectors=healpix_base_directions())
