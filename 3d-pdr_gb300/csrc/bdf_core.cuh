@@ -37,15 +37,43 @@ constexpr int FELL_BACK = 1;   // internal status: redo this cell in FP64
 // failure within one step sends the cell to the FP64 pass
 constexpr int MIXED_RETRIES = 3;
 
-// shared memory of one integrator: arrays every thread reads
+// shared memory of one integrator: arrays every thread reads.  The error
+// constants tq[1..5] are kept in the norm type (tqf in the mixed form, tqd in
+// FP64), and the mixed form mirrors the step history in FP32 (tauf), so that
+// its FP32 coefficient recurrence and threshold tests read them without
+// conversions: on GB300 an F2F costs an FP64 issue slot like a DFMA.
 struct CoefShared {
   double tau[QMAX + 2];
   double l[QMAX + 1];
-  double tq[6];   // tq[0] = 1/l[1], tq[1..5] error constants
+  double rl1;     // 1/l[1]
   // coefficients of a uniform step history (xi_j = j), per order 1..5
   double ul[QMAX + 1][QMAX + 1];
-  double utq[QMAX + 1][6];
+  double url1[QMAX + 1];
+  double tqd[6], utqd[QMAX + 1][6];
+  float tqf[6], utqf[QMAX + 1][6], tauf[QMAX + 2];
 };
+
+// Comparisons of uniform FP64 scalars in integer arithmetic: for operands
+// whose sign bits are clear, the bit patterns order like the values, and NaN
+// (any payload) compares false as in FP.  A set sign bit takes the FP compare.
+__device__ __forceinline__ bool nan_bits(unsigned long long b) {
+  return (b & 0x7FFFFFFFFFFFFFFFull) > 0x7FF0000000000000ull;
+}
+__device__ __forceinline__ bool ge_u(double a, double b) {
+  const unsigned long long x = __double_as_longlong(a), y = __double_as_longlong(b);
+  if ((x | y) >> 63) return a >= b;
+  return x >= y && !nan_bits(x) && !nan_bits(y);
+}
+__device__ __forceinline__ bool lt_u(double a, double b) {
+  const unsigned long long x = __double_as_longlong(a), y = __double_as_longlong(b);
+  if ((x | y) >> 63) return a < b;
+  return x < y && !nan_bits(x) && !nan_bits(y);
+}
+__device__ __forceinline__ bool eq_u(double a, double b) {
+  const unsigned long long x = __double_as_longlong(a), y = __double_as_longlong(b);
+  if ((x | y) >> 63) return a == b;
+  return x == y && !nan_bits(x);
+}
 
 // squared-norm form of eta = 1/((bias*e)^(1/k) + 1e-6) with e2 = e^2 (FP32)
 __device__ __forceinline__ double eta_of(float e2, float bias, int k) {
@@ -110,13 +138,28 @@ struct Core {
   NT ewt;
   double acor, y, ftmp, tmp;
   // uniform integrator scalars
-  double tn, h, hscale, hprime, eta, etamax, saved_tq5, gamma, gammap, rl1;
-  NT inv_gammap, gamrat, gscale;
+  double tn, h, hscale, hprime, eta, etamax, gamma, gammap, rl1;
+  NT inv_gammap, gamrat, gscale, saved_tq5;
+  NT h_nt;   // h in the norm type, set with the coefficients
   NT crate2, acnrm2;
   double xe_last, rtol, atol;
   int q, qprime, qwait, jcur;
   int nst, nstlp, nfe, nje, nsetups, nni, ncfn, netf;
   long long mxstep, max_total_steps;
+
+  // the error constants and step history in the norm type
+  __device__ __forceinline__ NT *tqn() const {
+    if constexpr (NORM32) return ws->tqf;
+    else return ws->tqd;
+  }
+  __device__ __forceinline__ NT utqn(int qq, int j) const {
+    if constexpr (NORM32) return ws->utqf[qq][j];
+    else return ws->utqd[qq][j];
+  }
+  __device__ __forceinline__ const NT *taun() const {
+    if constexpr (NORM32) return ws->tauf;
+    else return ws->tau;
+  }
 
   __device__ __forceinline__ NT wrms2(double v) {
     const NT t = self().owns ? (NT)v * ewt : NT(0);
@@ -225,7 +268,7 @@ struct Core {
   // solution by ~1e-7 of the correction (itself of the size of the local
   // error), and the ~10 divisions here cost FP32 instead of FP64 issue slots
   template <class T>
-  __device__ __forceinline__ static void coeffs(int q, bool order_change_due, T h, const double *tau, T *l, T *tq) {
+  __device__ __forceinline__ static void coeffs(int q, bool order_change_due, T h, const T *tau, T *l, T *tq) {
 #pragma unroll
     for (int j = 0; j <= QMAX; j++) l[j] = T(0);
     l[0] = l[1] = T(1);
@@ -234,7 +277,7 @@ struct Core {
 #pragma unroll
       for (int j = 2; j < QMAX; j++) {
         if (j < q) {
-          hsum += (T)tau[j - 1];
+          hsum += tau[j - 1];
           xi_inv = h / hsum;
           a0 -= T(1) / T(j);
 #pragma unroll
@@ -244,7 +287,7 @@ struct Core {
       }
       a0 -= T(1) / T(q);
       xistar_inv = -l[1] - a0;
-      hsum += (T)tau[q - 1];
+      hsum += tau[q - 1];
       xi_inv = h / hsum;
       a0hat = -l[1] - xi_inv;
 #pragma unroll
@@ -264,7 +307,7 @@ struct Core {
       } else {
         tq[1] = T(1);
       }
-      hsum += (T)tau[q];
+      hsum += tau[q];
       xi_inv = h / hsum;
       const T A5 = a0 - T(1) / T(q + 1), A6 = a0hat - xi_inv;
       tq[3] = fabs(((T(1) - A6 + A5) / A2) / (xi_inv * T(q + 2) * A5));
@@ -283,44 +326,65 @@ struct Core {
       self().sync();
       if (self().leader()) {
         for (int j = 0; j <= QMAX; j++) ws->ul[qq][j] = l[j];
-        ws->utq[qq][0] = 1.0 / l[1];
-        for (int j = 1; j <= 5; j++) ws->utq[qq][j] = tq[j];
+        ws->url1[qq] = 1.0 / l[1];
+        for (int j = 1; j <= 5; j++) {
+          ws->utqd[qq][j] = tq[j];
+          ws->utqf[qq][j] = (float)tq[j];
+        }
       }
     }
     self().sync();
   }
 
+  // store l[0..Q] of the FP32/FP64 recurrence as FP64 (only the used terms)
+  template <int Q>
+  __device__ __forceinline__ void store_l(const NT *l) {
+#pragma unroll
+    for (int j = 0; j <= Q; j++) ws->l[j] = (double)l[j];
+  }
+
   __device__ __forceinline__ void set_coeffs() {
     // a history of equal steps gives xi_j = j exactly: take the tabulated values
     bool uniform = true;
+    const unsigned long long hb = __double_as_longlong(h);
 #pragma unroll
     for (int j = 1; j <= QMAX; j++)
-      if (j <= q && ws->tau[j] != h) uniform = false;
+      if (j <= q && (unsigned long long)__double_as_longlong(ws->tau[j]) != hb) uniform = false;
     self().sync();
+    NT *tq = tqn();
     if (uniform) {
+      // h equals tau[1] bit for bit, so its FP32 value is the mirror's
+      if constexpr (NORM32) h_nt = ws->tauf[1];
+      else h_nt = h;
       if (self().leader()) {
 #pragma unroll
         for (int j = 0; j <= QMAX; j++) ws->l[j] = ws->ul[q][j];
-        ws->tq[0] = ws->utq[q][0];
-        ws->tq[2] = ws->utq[q][2];
-        ws->tq[4] = ws->utq[q][4];
-        ws->tq[5] = ws->utq[q][5];
-        if (qwait == 1) { ws->tq[1] = ws->utq[q][1]; ws->tq[3] = ws->utq[q][3]; }
+        ws->rl1 = ws->url1[q];
+        tq[2] = utqn(q, 2);
+        tq[4] = utqn(q, 4);
+        tq[5] = utqn(q, 5);
+        if (qwait == 1) { tq[1] = utqn(q, 1); tq[3] = utqn(q, 3); }
       }
     } else {
-      NT l[QMAX + 1], tq[6];
-      tq[1] = (NT)ws->tq[1];
-      tq[3] = (NT)ws->tq[3];
-      coeffs<NT>(q, qwait == 1, (NT)h, ws->tau, l, tq);
+      h_nt = (NT)h;
+      NT l[QMAX + 1], tqv[6];
+      tqv[1] = tq[1];
+      tqv[3] = tq[3];
+      coeffs<NT>(q, qwait == 1, h_nt, taun(), l, tqv);
       if (self().leader()) {
-#pragma unroll
-        for (int j = 0; j <= QMAX; j++) ws->l[j] = l[j];
-        ws->tq[0] = NT(1) / l[1];
-        ws->tq[1] = tq[1]; ws->tq[2] = tq[2]; ws->tq[3] = tq[3]; ws->tq[4] = tq[4]; ws->tq[5] = tq[5];
+        switch (q) {
+          case 1: store_l<1>(l); break;
+          case 2: store_l<2>(l); break;
+          case 3: store_l<3>(l); break;
+          case 4: store_l<4>(l); break;
+          default: store_l<5>(l); break;
+        }
+        ws->rl1 = (double)(NT(1) / l[1]);
+        tq[1] = tqv[1]; tq[2] = tqv[2]; tq[3] = tqv[3]; tq[4] = tqv[4]; tq[5] = tqv[5];
       }
     }
     self().sync();
-    rl1 = ws->tq[0];
+    rl1 = ws->rl1;
     gamma = h * rl1;
     if (nst == 0) { gammap = gamma; inv_gammap = NT(1) / (NT)gamma; }
     gamrat = (nst > 0) ? (NT)gamma * inv_gammap : NT(1);
@@ -344,7 +408,7 @@ struct Core {
   // 0 solved, 1 convergence failure, 2 failure that sends the cell to the FP64 pass
   __device__ __forceinline__ int nls(bool prev_fail, bool fallback_on_fail) {
     bool call_setup = prev_fail || (nst == 0) || (nst >= nstlp + MSBP) || (fabs(gamrat - NT(1)) > NT(DGMAX));
-    const NT tq4 = (NT)ws->tq[4];
+    const NT tq4 = tqn()[4];
     const NT tq4sq = tq4 * tq4;
     const int fail = fallback_on_fail ? 2 : 1;
     for (int attempt = 0; attempt < 2; attempt++) {
@@ -387,7 +451,7 @@ struct Core {
   }
 
   __device__ __forceinline__ void set_eta() {
-    if (eta < THRESH) { eta = 1.0; hprime = h; }
+    if (lt_u(eta, THRESH)) { eta = 1.0; hprime = h; }
     else { eta = fmin(eta, etamax); hprime = h * eta; }
   }
 
@@ -397,7 +461,7 @@ struct Core {
     int ncf = 0, nef = 0;
     bool prev_fail = false;
     NT dsm2 = 0;
-    if (nst > 0 && hprime != h) {
+    if (nst > 0 && !eq_u(hprime, h)) {
       if (qprime != q) {
         if (qprime > q) increase_order();
         else decrease_order();
@@ -422,7 +486,7 @@ struct Core {
         rescale();
         continue;
       }
-      const NT tq2 = (NT)ws->tq[2];
+      const NT tq2 = tqn()[2];
       dsm2 = acnrm2 * (tq2 * tq2);
       if (dsm2 <= NT(1)) break;
       nef++;
@@ -463,6 +527,14 @@ struct Core {
         if (i <= q) ws->tau[i] = ws->tau[i - 1];
       if (q == 1 && nst > 1) ws->tau[2] = ws->tau[1];
       ws->tau[1] = h;
+      if constexpr (NORM32) {
+        // the FP32 mirror: h_nt is (float)h of the coefficients of this step
+#pragma unroll
+        for (int i = QMAX; i >= 2; i--)
+          if (i <= q) ws->tauf[i] = ws->tauf[i - 1];
+        if (q == 1 && nst > 1) ws->tauf[2] = ws->tauf[1];
+        ws->tauf[1] = h_nt;
+      }
     }
     self().sync();
     switch (q) {
@@ -473,9 +545,9 @@ struct Core {
     qwait--;
     if (qwait == 1 && q != QMAX) {
       z[QMAX] = acor;
-      saved_tq5 = ws->tq[5];
+      saved_tq5 = tqn()[5];
     }
-    if (etamax == 1.0) {
+    if (eq_u(etamax, 1.0)) {
       if (qwait < 2) qwait = 2;
       qprime = q;
       hprime = h;
@@ -494,16 +566,18 @@ struct Core {
           double zq = 0.0;
 #pragma unroll
           for (int j = 0; j <= QMAX; j++) if (j == q) zq = z[j];
-          const NT tq1 = (NT)ws->tq[1];
+          const NT tq1 = tqn()[1];
           etaqm1 = eta_of(wrms2(zq) * (tq1 * tq1), (float)BIAS1, q);
         }
-        if (q != QMAX && saved_tq5 != 0.0) {
+        if (q != QMAX && saved_tq5 != NT(0)) {
           // step-ratio factor of the order-raise estimate (heuristic, FP32)
-          const float ratio = (float)h / (float)ws->tau[2];
+          float ratio;
+          if constexpr (NORM32) ratio = h_nt / ws->tauf[2];
+          else ratio = (float)h / (float)ws->tau[2];
           float rp = ratio;
           for (int k = 1; k < L; k++) rp *= ratio;
-          const double cquot = (double)(((float)ws->tq[5] / (float)saved_tq5) * rp);
-          const NT tq3 = (NT)ws->tq[3];
+          const double cquot = (double)(((float)tqn()[5] / (float)saved_tq5) * rp);
+          const NT tq3 = tqn()[3];
           etaqp1 = eta_of(wrms2(acor - cquot * z[QMAX]) * (tq3 * tq3), (float)BIAS3, L + 1);
         }
         // ties keep the current order, then prefer the lower one
@@ -568,7 +642,7 @@ struct Core {
       qwait = 2;
       etamax = ETAMX1;
       nst = 0;
-    } else if (tn >= tout) {   // h > 0: the integration runs forward
+    } else if (ge_u(tn, tout)) {   // h > 0: the integration runs forward
       return 0;
     }
     long long nstloc = 0;
@@ -579,7 +653,7 @@ struct Core {
       if (kf != 0) return kf;
       nstloc++;
       total++;
-      if (tn >= tout) return 0;
+      if (ge_u(tn, tout)) return 0;
     }
   }
 
@@ -590,14 +664,14 @@ struct Core {
   __device__ __forceinline__ int integrate(double t0_yr, double tend_yr, bool fb, double *yout) {
     if (self().leader()) {
 #pragma unroll
-      for (int j = 0; j < QMAX + 2; j++) ws->tau[j] = 0.0;
+      for (int j = 0; j < QMAX + 2; j++) { ws->tau[j] = 0.0; ws->tauf[j] = 0.0f; }
 #pragma unroll
-      for (int j = 0; j < 6; j++) ws->tq[j] = 0.0;
+      for (int j = 0; j < 6; j++) { ws->tqd[j] = 0.0; ws->tqf[j] = 0.0f; }
     }
     self().sync();
     nfe = nje = nsetups = nni = ncfn = netf = 0;
     nst = nstlp = 0;
-    saved_tq5 = 0.0;
+    saved_tq5 = NT(0);
     crate2 = 1.0;
     gammap = gamma = 1.0;
     inv_gammap = 1.0;
