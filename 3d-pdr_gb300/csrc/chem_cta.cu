@@ -267,19 +267,41 @@ struct CtaCell : Core<CtaCell<MIXED>, false, MIXED> {
     if (owns)
       for (int j = 0; j < n + 2; j++) M(tid, j) = MT(0);
     __syncthreads();
-    if (owns) {
-      // the term tables are read from L2: keep several loads in flight
-#pragma unroll 8
-      for (int t = 0; t < T.jac_len; t++) {
+    // J entries term-parallel: every thread sums its balanced chunk of the
+    // entry-sorted contributions in a register (rows with thousands of terms
+    // no longer serialise on one thread); runs crossing a chunk boundary are
+    // added up from their slots, in chunk order, by a second pass
+    {
+      MT *slots = upan;   // the LU panel buffer is free during the assembly
+      MT s = MT(0);
+#pragma unroll 4
+      for (int t = 0; t < T.hlen; t++) {
+        const int x = __ldg(&T.h_x[t * G + tid]);
+        const int y = __ldg(&T.h_y[t * G + tid]);
         MT nu;
-        if constexpr (MIXED) nu = __ldg(&T.jac_nu_f[t * G + tid]);
-        else nu = __ldg(&T.jac_nu[t * G + tid]);
-        if (nu == MT(0)) break;
-        const int rab = __ldg(&T.jac_rab[t * G + tid]);
-        const int r = rab & 0xffff, a = (rab >> 16) & 0xff, b = (rab >> 24) & 0xff;
-        M(tid, a) = fma(nu, Da[r], M(tid, a));
-        M(tid, b) = fma(nu, Db[r], M(tid, b));
+        if constexpr (MIXED) nu = __ldg(&T.h_nu_f[t * G + tid]);
+        else nu = __ldg(&T.h_nu[t * G + tid]);
+        const int r = x & 0xffff;
+        s = fma(nu, (x & 0x10000) ? Db[r] : Da[r], s);
+        const int kind = (x >> 17) & 3;
+        if (kind == 1) {
+          M(y & 0xff, (y >> 8) & 0xff) = s;
+          s = MT(0);
+        } else if (kind == 2) {
+          slots[y >> 16] = s;
+          s = MT(0);
+        }
       }
+      __syncthreads();
+      for (int b = tid; b < T.nbnd; b += G) {
+        const int tt = __ldg(&T.bnd_t[b]), ss = __ldg(&T.bnd_s[b]);
+        MT acc = MT(0);
+        for (int q = ss & 0xffff; q < (ss >> 16); q++) acc += slots[q];
+        M(tt & 0xff, (tt >> 8) & 0xff) = acc;
+      }
+      __syncthreads();
+    }
+    if (owns) {
       const MT e = M(tid, n);
       MT rf;
       if constexpr (MIXED) rf = (MT)(rf_d * (wsc * this->atol));

@@ -45,6 +45,19 @@ struct WarpTables {
   double *jac_nu = nullptr;   // [jac_len][lanes]
   float *jac_nu_f = nullptr;  // [jac_len][lanes]
   double *xe_coef = nullptr;  // [lanes] electron-sum coefficient per slot
+  // term-parallel Jacobian assembly (block integrator): the (row, column)
+  // contributions nu * dphi_r/dx_col of every term, sorted by entry and cut
+  // into `lanes` balanced chunks; a chunk sums each run of one entry in a
+  // register and stores it (kind 1), or, for a run that crosses a chunk
+  // boundary, leaves its partial in a boundary slot (kind 2) that a second
+  // pass adds up in chunk order
+  int hlen = 0, nbnd = 0;
+  int *h_x = nullptr;         // [hlen][lanes] reaction | Db? << 16 | kind << 17 (0 accumulate, 1 store, 2 slot)
+  int *h_y = nullptr;         // [hlen][lanes] row | column << 8 | slot << 16
+  double *h_nu = nullptr;     // [hlen][lanes] nu (0 = padding)
+  float *h_nu_f = nullptr;
+  int *bnd_t = nullptr;       // [nbnd] row | column << 8 of a boundary entry
+  int *bnd_s = nullptr;       // [nbnd] first slot | (last slot + 1) << 16
 };
 
 // Device tables for the rate evaluator.

@@ -286,6 +286,62 @@ int build_device_tables(pdr_net *net) {
       }
     std::vector<double> xe(G, 0.0);
     for (int i = 0; i < neq; i++) xe[i] = h.xe[i];
+    // term-parallel Jacobian tables (block integrator only)
+    std::vector<int> hx, hy, bt, bs;
+    std::vector<double> hn;
+    std::vector<float> hnf;
+    if (G > kWarp) {
+      struct Half { int i, col, r, which; double nu; };
+      std::vector<Half> hs;
+      for (auto &t : terms) {
+        const int2 ab = rab[t.r];
+        if (ab.x <= neq) hs.push_back({t.i, ab.x, t.r, 0, t.nu});   // column a: Da
+        if (ab.y <= neq) hs.push_back({t.i, ab.y, t.r, 1, t.nu});   // column b: Db
+      }
+      std::stable_sort(hs.begin(), hs.end(), [](const Half &x, const Half &y) {
+        if (x.i != y.i) return x.i < y.i;
+        if (x.col != y.col) return x.col < y.col;
+        if (x.r != y.r) return x.r < y.r;
+        return x.which < y.which;
+      });
+      const int H = (int)hs.size();
+      w.hlen = std::max(1, (H + G - 1) / G);
+      hx.assign((size_t)w.hlen * G, 0);
+      hy.assign((size_t)w.hlen * G, 0);
+      hn.assign((size_t)w.hlen * G, 0.0);
+      hnf.assign((size_t)w.hlen * G, 0.0f);
+      // an entry's runs: the chunks holding it, in order
+      int slot = 0;
+      for (int e0 = 0; e0 < H;) {
+        int e1 = e0;
+        while (e1 < H && hs[e1].i == hs[e0].i && hs[e1].col == hs[e0].col) e1++;
+        const int c0 = e0 / w.hlen, c1 = (e1 - 1) / w.hlen;
+        const int first_slot = slot;
+        for (int c = c0; c <= c1; c++) {
+          const int b = std::max(e0, c * w.hlen), e = std::min(e1, (c + 1) * w.hlen);
+          for (int k = b; k < e; k++) {
+            const int t = k - c * w.hlen;
+            int kind = 0, sl = 0;
+            if (k + 1 == e) {
+              kind = (c0 == c1) ? 1 : 2;
+              if (kind == 2) sl = slot++;
+            }
+            hx[(size_t)t * G + c] = hs[k].r | (hs[k].which << 16) | (kind << 17);
+            hy[(size_t)t * G + c] = hs[k].i | (hs[k].col << 8) | (sl << 16);
+            hn[(size_t)t * G + c] = hs[k].nu;
+            hnf[(size_t)t * G + c] = (float)hs[k].nu;
+          }
+        }
+        if (c0 != c1) {
+          bt.push_back(hs[e0].i | (hs[e0].col << 8));
+          bs.push_back(first_slot | (slot << 16));
+        }
+        e0 = e1;
+      }
+      // the slots live in the block integrator's LU panel buffer (8 x neq values)
+      if (slot > 8 * neq || neq + 1 > 255) return PDR_E_NET;
+      w.nbnd = (int)bt.size();
+    }
     int rc2 = 0;
     w.rab = upload(net, rab, rc2);
     w.nh_mask = upload(net, nhm, rc2);
@@ -296,6 +352,16 @@ int build_device_tables(pdr_net *net) {
     w.jac_nu = upload(net, jn, rc2);
     w.jac_nu_f = upload(net, jnf, rc2);
     w.xe_coef = upload(net, xe, rc2);
+    if (G > kWarp) {
+      w.h_x = upload(net, hx, rc2);
+      w.h_y = upload(net, hy, rc2);
+      w.h_nu = upload(net, hn, rc2);
+      w.h_nu_f = upload(net, hnf, rc2);
+      if (!bt.empty()) {
+        w.bnd_t = upload(net, bt, rc2);
+        w.bnd_s = upload(net, bs, rc2);
+      }
+    }
     return rc2;
   };
   if (neq <= kWarp) {
