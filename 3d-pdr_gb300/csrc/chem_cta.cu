@@ -321,6 +321,26 @@ struct CtaCell : Core<CtaCell<MIXED>, false, MIXED> {
     else return __frcp_rn(x);
   }
 
+  // the PB U-panel entries of column jj (16-byte aligned: upan is, and a
+  // column holds PB = 8 values)
+  __device__ __forceinline__ void load_upan(int jj, MT (&u)[PB]) const {
+    if constexpr (sizeof(MT) == 4) {
+      const float4 *p = reinterpret_cast<const float4 *>(upan + (size_t)jj * PB);
+#pragma unroll
+      for (int q = 0; q < PB / 4; q++) {
+        const float4 v = p[q];
+        u[4 * q] = v.x; u[4 * q + 1] = v.y; u[4 * q + 2] = v.z; u[4 * q + 3] = v.w;
+      }
+    } else {
+      const double2 *p = reinterpret_cast<const double2 *>(upan + (size_t)jj * PB);
+#pragma unroll
+      for (int q = 0; q < PB / 2; q++) {
+        const double2 v = p[q];
+        u[2 * q] = v.x; u[2 * q + 1] = v.y;
+      }
+    }
+  }
+
   // LU with partial pivoting in place; false if a column has no nonzero pivot
   __device__ __forceinline__ bool lu() {
     mystep = owns ? -1 : n;
@@ -384,12 +404,33 @@ struct CtaCell : Core<CtaCell<MIXED>, false, MIXED> {
           any |= (l[t] != MT(0));
         }
         if (any) {
-#pragma unroll 4
-          for (int c = 0; c < ncols; c++) {
-            const int jj = cols[c];
-            MT s = M(tid, jj);
+          // four columns at a time: every load of the group is issued before
+          // any store (the compiler cannot prove the panel buffer and the
+          // matrix apart), the U entries of a column as 16-byte vectors
+          constexpr int CB = 4;
+          int c = 0;
+          for (; c + CB <= ncols; c += CB) {
+            int jj[CB];
+            MT s[CB], u[CB][PB];
 #pragma unroll
-            for (int t = 0; t < PB; t++) s = fma(-l[t], upan[(size_t)jj * PB + t], s);
+            for (int b = 0; b < CB; b++) {
+              jj[b] = cols[c + b];
+              s[b] = M(tid, jj[b]);
+              load_upan(jj[b], u[b]);
+            }
+#pragma unroll
+            for (int b = 0; b < CB; b++) {
+#pragma unroll
+              for (int t = 0; t < PB; t++) s[b] = fma(-l[t], u[b][t], s[b]);
+              M(tid, jj[b]) = s[b];
+            }
+          }
+          for (; c < ncols; c++) {
+            const int jj = cols[c];
+            MT s = M(tid, jj), u[PB];
+            load_upan(jj, u);
+#pragma unroll
+            for (int t = 0; t < PB; t++) s = fma(-l[t], u[t], s);
             M(tid, jj) = s;
           }
         }
