@@ -286,7 +286,8 @@ int build_device_tables(pdr_net *net) {
       }
     std::vector<double> xe(G, 0.0);
     for (int i = 0; i < neq; i++) xe[i] = h.xe[i];
-    // term-parallel Jacobian tables (block integrator only)
+    // term-parallel Jacobian tables (block integrator only: in the warp
+    // integrator the per-row lists measured as fast)
     std::vector<int> hx, hy, bt, bs;
     std::vector<double> hn;
     std::vector<float> hnf;
