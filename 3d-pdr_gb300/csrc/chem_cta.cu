@@ -12,14 +12,16 @@
 //   RHS  fluxes phi_r = kn_r x_a x_b reaction-parallel over the block, the
 //        stoichiometric sums in G balanced chunks with deterministic partial
 //        sums (the same scheme as the warp integrator, stride G);
-//   Jac  thread i accumulates row i from its term list, then the x_e chain
-//        rule J_ij += (df_i/dx_e) c_j;
+//   Jac  the entry-sorted term contributions in G balanced chunks, one
+//        register sum per entry run (runs across chunks added in chunk
+//        order), then the x_e chain rule J_ij += (df_i/dx_e) c_j by row;
 //   LU   dense LU with partial pivoting (CVDense semantics: in each column the
 //        unpivoted row of largest magnitude, lowest row on ties), rows kept in
 //        place with the pivot order recorded; right-looking in panels of 8
 //        columns: per panel the pivot rows' U block is formed column-parallel
-//        and the trailing update is a rank-8 update applied by the row owners
-//        to the columns where that U block has a nonzero (the network's
+//        and the trailing update is a rank-8 update applied by the row owners,
+//        four columns at a time, to the columns where that U block has a
+//        nonzero (the network's
 //        Jacobian is sparse, so many are exactly zero -- skipping them changes
 //        no result);
 //   solve forward/backward substitution in 32-row blocks: the 32x32 diagonal
