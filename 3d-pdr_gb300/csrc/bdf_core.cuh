@@ -33,9 +33,10 @@ constexpr double ETACF = 0.25, ADDON = 1e-6, BIAS1 = 6.0, BIAS2 = 6.0, BIAS3 = 1
 constexpr double YEAR = 3.1556926e7;
 constexpr int FELL_BACK = 1;   // internal status: redo this cell in FP64
 // mixed form: a Newton failure with a fresh FP32 matrix is first handled as a
-// convergence failure (step size x 0.25, as CVODE does); the third such
-// failure within one step sends the cell to the FP64 pass
-constexpr int MIXED_RETRIES = 3;
+// convergence failure (step size x 0.25, as CVODE does); the fifth such
+// failure within one step sends the cell to the FP64 pass (on the full
+// network, three retries sent 0.3 % of cells there, five send none)
+constexpr int MIXED_RETRIES = 5;
 
 // shared memory of one integrator: arrays every thread reads.  The error
 // constants tq[1..5] are kept in the norm type (tqf in the mixed form, tqd in
