@@ -183,6 +183,14 @@ struct Core {
   }
   template <int SIGN>
   __device__ __forceinline__ void pascal_q() {
+    if constexpr (ZSHARED) {
+      // rows in shared memory: a rolled loop keeps the step's code small
+#pragma unroll 1
+      for (int k = 1; k <= q; k++)
+#pragma unroll 1
+        for (int j = q; j >= k; j--) z[j - 1] = (SIGN > 0) ? z[j - 1] + z[j] : z[j - 1] - z[j];
+      return;
+    }
     switch (q) {
       case 1: pascal<1, SIGN>(); break;
       case 2: pascal<2, SIGN>(); break;
@@ -538,7 +546,10 @@ struct Core {
       }
     }
     self().sync();
-    switch (q) {
+    if constexpr (ZSHARED) {
+#pragma unroll 1
+      for (int j = 0; j <= q; j++) z[j] = fma(ws->l[j], acor, z[j]);
+    } else switch (q) {
 #define PDR_CORRECT(Q) case Q: _Pragma("unroll") for (int j = 0; j <= Q; j++) z[j] = fma(ws->l[j], acor, z[j]); break;
       PDR_CORRECT(1) PDR_CORRECT(2) PDR_CORRECT(3) PDR_CORRECT(4) PDR_CORRECT(5)
 #undef PDR_CORRECT

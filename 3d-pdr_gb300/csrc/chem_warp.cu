@@ -108,6 +108,7 @@ template <int N, class MT>
 __device__ __forceinline__ bool lu_rows(MT *a, int ld, int lane, int &mystep, MT &invd, int *perm) {
   mystep = (lane < N) ? -1 : N;
   MT *row = a + lane * ld;
+#pragma unroll 1
   for (int k = 0; k < N; k++) {
     const bool cand = (mystep < 0);
     const int p = argmax_lane(cand ? fabs(row[k]) : MT(0), cand);
@@ -133,11 +134,13 @@ template <int N, class MT>
 __device__ __forceinline__ MT lu_solve_rows(const MT *a, int ld, int lane, int mystep, MT invd, MT b,
                                             const int *perm) {
   const MT *row = a + (lane < N ? lane : 0) * ld;
+#pragma unroll 4
   for (int k = 0; k < N; k++) {
     const MT yk = bcast(b, perm[k]);
     if (mystep > k) b = fma(-row[k], yk, b);
   }
   MT x = MT(0);
+#pragma unroll 4
   for (int k = N - 1; k >= 0; k--) {
     const MT xk = bcast(b * invd, perm[k]);
     if (lane == k) x = xk;
@@ -186,7 +189,7 @@ struct WarpCell : Core<WarpCell<NSP, MIXED, ZSH>, ZSH, MIXED> {
     }
     __syncwarp();
     double s = 0.0;
-#pragma unroll 4
+#pragma unroll 2
     for (int t = 0; t < T.rhs_len; t++) {
       const int rf = __ldg(&T.rhs_rf[t * kWarp + lane]);
       const double nu = __ldg(&T.rhs_nu[t * kWarp + lane]);
@@ -251,7 +254,7 @@ struct WarpCell : Core<WarpCell<NSP, MIXED, ZSH>, ZSH, MIXED> {
     MT rf;
     if constexpr (MIXED) rf = (MT)(rf_d * (wsc * this->atol));   // row weight, normalised like the columns
     else rf = (MT)rf_d;
-#pragma unroll
+#pragma unroll 4
     for (int j = 0; j < NSP; j++) {
       const MT cj = (MT)__ldg(&T.xe_coef[j]);
       MT v = owns ? row[j] : MT(0);
