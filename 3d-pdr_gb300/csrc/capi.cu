@@ -499,7 +499,7 @@ int pdr_chem_eval_batched(const pdr_net *net, int nstate, const double *d_x, con
     return PDR_E_ARG;
   }
   if (!net->warp_ok || net->host.neq != 32) {
-    set_error("pdr_chem_eval_batched: this build evaluates networks with 32 ODE species");
+    set_error("pdr_chem_eval_batched: only networks with 32 ODE species are evaluated");
     return PDR_E_NET;
   }
   if (nstate == 0) return 0;
