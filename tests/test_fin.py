@@ -126,3 +126,30 @@ def test_benchmark_files_rewrite_byte_for_byte(benchmarks, tmp_path, case):
     assert np.array_equal(op[:, 1], t[:, 1])
     F.opdp_fin(out("opdp"), op[:, 1], _lines_from(op[:, 2:], nrays=12))
     assert same("opdp")
+
+
+def test_three_dimensional_layouts(tmp_path):
+    """The non-PSEUDO_1D records (3DPDR.F90:1283-1285, 1411-1418): x, y, z instead
+    of x, A_V(6), and the A_V of every ray at the end of the record."""
+    n, nrays = 3, 12
+    x, y, z = np.array([0.1, 0.2, 0.3]), np.array([1.0, 2.0, 3.0]), np.array([-1.0, -2.0, -3.0])
+    ab = np.full((n, 33), 1.0e-5)
+    AV = np.arange(n * nrays, dtype=float).reshape(n, nrays) + 0.5
+    p = tmp_path / "x.pdr.fin"
+    F.pdr_fin(str(p), x, None, [10.0, 20.0, 30.0], [5.0, 5.0, 5.0], [1, 1, 2], [1e3, 1e3, 1e3], [1.0, 2.0, 3.0],
+              ab, pseudo1d=False, y=y, z=z, AV=AV)
+    rows = p.read_text().splitlines()
+    assert len(rows) == n and all(len(r) == 7 + 5 * 11 + 5 + (2 + 33 + nrays) * 11 for r in rows)
+    # records of the last two cells come in the order n, n-1
+    assert [int(r[:7]) for r in rows] == [1, 3, 2]
+    r = rows[0]
+    assert r[7:18] == F.es(0.1) and r[18:29] == F.es(1.0) and r[29:40] == F.es(-1.0)
+    assert int(r[62:67]) == 1 and r[-11:] == F.es(AV[0, -1])
+    lines = {k: np.zeros((n, 41 if k == "CO" else 5, 41 if k == "CO" else 5)) for k in F.COOLANTS}
+    lines["CII"][:, 1, 0] = [7.0, 8.0, 9.0]
+    q = tmp_path / "x.line.fin"
+    F.line_fin(str(q), x, None, lines, pseudo1d=False, y=y, z=z, AV=AV)
+    rows = q.read_text().splitlines()
+    assert [int(r[:9]) for r in rows] == [1, 3, 2]
+    assert all(len(r) == 9 + (3 + 17 + nrays) * 11 for r in rows)
+    assert rows[1][9 + 3 * 11:9 + 4 * 11] == F.es(9.0)
