@@ -151,3 +151,19 @@ def test_level_populations_and_cooling(case):
         assert np.median(rp) < 1e-2 and np.percentile(rp, 90) < 6e-2, key
     rt = rel(total, d["cool"][:, 4])
     assert np.median(rt) < 1e-3 and np.percentile(rt, 90) < 1e-2
+
+
+def test_slab_rays_geometry():
+    """workloads.slab_rays: ray 6 of each cell runs from the cell through every
+    point nearer the x = 0 face, farthest first; the other rays are empty."""
+    x = np.array([0.3, 0.0, 0.7, 0.1, 0.5])
+    r = W.slab_rays(x)
+    ep = r["epray"].reshape(len(x), 12)
+    off = r["offset"].reshape(len(x), 12)
+    assert np.all(np.delete(ep, 6, axis=1) == 0)
+    for c in range(len(x)):
+        pts = r["gridpoint"][off[c, 6]:off[c, 6] + ep[c, 6] + 1]
+        assert pts[0] == c
+        assert list(x[pts[1:]]) == sorted(x[x < x[c]], reverse=True)
+        assert np.array_equal(r["xyz"][off[c, 6]:off[c, 6] + ep[c, 6] + 1, 0], x[pts])
+    assert r["npoint"] == len(r["gridpoint"]) and np.allclose(r["vectors"][6], [-1.0, 0.0, 0.0])
