@@ -40,10 +40,12 @@ size_t chem_cta_global_bytes(const pdr_net *net, bool mixed, int grid);
 size_t chem_cta_smem(const pdr_net *net, bool mixed, bool *mat_smem);
 int chem_cta_blocks_per_sm(const pdr_net *net, bool mixed);
 int launch_rates(const pdr_net *net, const pdr_phys &ph, int ncell, int nrays, const double *T,
-                 const double *Td, const double *rad, const double *AV, const double *col5, double *rate,
-                 int *status, int sm_count, cudaStream_t st);
+                 const double *Td, const double *rad, const double *AV, const double *col5, const double *zeta,
+                 double *rate, int *status, int sm_count, cudaStream_t st);
 int launch_chem_eval(const pdr_net *net, int nstate, const double *x, const double *rate, const double *dens,
                      double *out, double *xe_out, int mode, cudaStream_t st);
+int launch_chem_eval_cta(const pdr_net *net, int nstate, const double *x, const double *rate, const double *dens,
+                         double *out, double *xe_out, int mode, cudaStream_t st);
 int upload_shield_tables(int dev);
 int build_coolant_tables(pdr_coolant *c);
 int launch_levpop(const pdr_coolant *c, const LevArgsHost &h, bool mixed, int sm_count, cudaStream_t st);
@@ -58,7 +60,7 @@ int launch_lte(const pdr_coolant *c, int ncell, const double *T, const double *d
                int sm_count, cudaStream_t st);
 int launch_heating(const pdr_net *net, int network, const pdr_phys &ph, int ncell, const double *dens,
                    const double *Tg, const double *Td, const double *uv, const double *ab, const double *rate,
-                   double *out, cudaStream_t st);
+                   const double *zeta, double *out, cudaStream_t st);
 void shield_tables_host(double *xderiv30, double *scoderiv48);
 int launch_thermal(const pdr_thermal_params &p, int level_conv, int first_time, const double *heat, int hstride,
                    int ncool, const double *const *cool, const pdr_thermal_state &s, double *total, int *nconv,
@@ -146,11 +148,11 @@ static int cta_per_sm(const pdr_net *net, bool mixed) {
 }
 
 
-static bool uses_warp_path(const pdr_net *net, const pdr_chem_opts &o) {
+bool uses_warp_path(const pdr_net *net, const pdr_chem_opts &o) {
   return (o.integrator == 1) || (o.integrator == 0 && net->warp_ok && net->host.neq == 32);
 }
 
-static int check_opts(const pdr_net *net, const pdr_chem_opts &o, const char *who) {
+int check_opts(const pdr_net *net, const pdr_chem_opts &o, const char *who) {
   if (!(o.reltol >= 0.0) || !(o.abstol > 0.0) || o.mxstep <= 0 ||
       (o.precision != PDR_FP64 && o.precision != PDR_MIXED) || o.integrator < 0 || o.integrator > 2) {
     set_error(std::string(who) + ": invalid options");
@@ -167,7 +169,7 @@ static int check_opts(const pdr_net *net, const pdr_chem_opts &o, const char *wh
 }
 
 // SMs the persistent grid spans
-static int eff_sms(const pdr_chem_opts &o, int sms) { return (o.max_sms > 0 && o.max_sms < sms) ? o.max_sms : sms; }
+int eff_sms(const pdr_chem_opts &o, int sms) { return (o.max_sms > 0 && o.max_sms < sms) ? o.max_sms : sms; }
 
 // grid of the block integrator for one precision
 static int cta_grid(const pdr_net *net, const pdr_chem_opts &o, bool mixed, int sms) {
@@ -472,9 +474,10 @@ int pdr_chem_autotune(const pdr_net *net, int ncell_sample, const double *d_abun
   return rc;
 }
 
-int pdr_rates_batched(const pdr_net *net, const pdr_phys *phys, int ncell, int nrays, const double *d_T,
-                      const double *d_Td, const double *d_rad_surface, const double *d_AV,
-                      const double *d_column5, double *d_rate, int *d_status, void *stream) {
+int pdr_rates_batched_cr(const pdr_net *net, const pdr_phys *phys, int ncell, int nrays, const double *d_T,
+                         const double *d_Td, const double *d_rad_surface, const double *d_AV,
+                         const double *d_column5, const double *d_zeta, double *d_rate, int *d_status,
+                         void *stream) {
   if (!net || !phys || ncell < 0 || nrays <= 0 || !d_T || !d_Td || !d_rad_surface || !d_AV ||
       !d_column5 || !d_rate) {
     set_error("pdr_rates_batched: invalid argument");
@@ -486,23 +489,35 @@ int pdr_rates_batched(const pdr_net *net, const pdr_phys *phys, int ncell, int n
   if (rc) return rc;
   rc = upload_shield_tables(dev);
   if (rc) return rc;
-  return launch_rates(net, *phys, ncell, nrays, d_T, d_Td, d_rad_surface, d_AV, d_column5, d_rate,
+  return launch_rates(net, *phys, ncell, nrays, d_T, d_Td, d_rad_surface, d_AV, d_column5, d_zeta, d_rate,
                       d_status, sms, (cudaStream_t)stream);
 }
 
+int pdr_rates_batched(const pdr_net *net, const pdr_phys *phys, int ncell, int nrays, const double *d_T,
+                      const double *d_Td, const double *d_rad_surface, const double *d_AV,
+                      const double *d_column5, double *d_rate, int *d_status, void *stream) {
+  return pdr_rates_batched_cr(net, phys, ncell, nrays, d_T, d_Td, d_rad_surface, d_AV, d_column5, nullptr, d_rate,
+                              d_status, stream);
+}
+
 // Diagnostic: the device RHS f(x) (mode 0, d_out[nstate*neq], d_xe[nstate]) or the
-// analytic Jacobian (mode 1, d_out[nstate*neq*neq] row-major) at given states.
+// analytic Jacobian (mode 1, d_out[nstate*neq*neq] row-major) at given states,
+// by the integrator the network runs on; modes 2 and 3 evaluate the same with
+// the block integrator's code for any network.
 int pdr_chem_eval_batched(const pdr_net *net, int nstate, const double *d_x, const double *d_rate,
                           const double *d_density, int mode, double *d_out, double *d_xe, void *stream) {
-  if (!net || nstate < 0 || !d_x || !d_rate || !d_density || !d_out || (mode != 0 && mode != 1)) {
+  if (!net || nstate < 0 || !d_x || !d_rate || !d_density || !d_out || mode < 0 || mode > 3) {
     set_error("pdr_chem_eval_batched: invalid argument");
     return PDR_E_ARG;
   }
-  if (!net->warp_ok || net->host.neq != 32) {
-    set_error("pdr_chem_eval_batched: only networks with 32 ODE species are evaluated");
+  const bool block = (mode >= 2) || !(net->warp_ok && net->host.neq == 32);
+  if (block && !net->cta_ok) {
+    set_error("pdr_chem_eval_batched: the network is too large for the integrator tables");
     return PDR_E_NET;
   }
   if (nstate == 0) return 0;
+  if (block)
+    return launch_chem_eval_cta(net, nstate, d_x, d_rate, d_density, d_out, d_xe, mode & 1, (cudaStream_t)stream);
   return launch_chem_eval(net, nstate, d_x, d_rate, d_density, d_out, d_xe, mode, (cudaStream_t)stream);
 }
 
@@ -619,6 +634,14 @@ int pdr_optical_depths_batched(const pdr_coolant *c, const pdr_rays *rays, const
 int pdr_heating_batched(const pdr_net *net, int network, const pdr_phys *phys, int ncell, const double *d_density,
                         const double *d_Tgas, const double *d_Tdust, const double *d_uv_field,
                         const double *d_abundance, const double *d_rate, double *d_heating, void *stream) {
+  return pdr_heating_batched_cr(net, network, phys, ncell, d_density, d_Tgas, d_Tdust, d_uv_field, d_abundance,
+                                d_rate, nullptr, d_heating, stream);
+}
+
+int pdr_heating_batched_cr(const pdr_net *net, int network, const pdr_phys *phys, int ncell, const double *d_density,
+                           const double *d_Tgas, const double *d_Tdust, const double *d_uv_field,
+                           const double *d_abundance, const double *d_rate, const double *d_zeta, double *d_heating,
+                           void *stream) {
   if (!net || !phys || ncell < 0 || !d_density || !d_Tgas || !d_Tdust || !d_uv_field || !d_abundance ||
       !d_rate || !d_heating) {
     set_error("pdr_heating_batched: invalid argument");
@@ -631,7 +654,7 @@ int pdr_heating_batched(const pdr_net *net, int network, const pdr_phys *phys, i
   }
   if (ncell == 0) return 0;
   return launch_heating(net, network, *phys, ncell, d_density, d_Tgas, d_Tdust, d_uv_field, d_abundance, d_rate,
-                        d_heating, (cudaStream_t)stream);
+                        d_zeta, d_heating, (cudaStream_t)stream);
 }
 
 int pdr_thermal_balance_batched(const pdr_thermal_params *params, int level_conv, int first_time,

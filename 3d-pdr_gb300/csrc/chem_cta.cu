@@ -241,8 +241,10 @@ struct CtaCell : Core<CtaCell<MIXED>, false, MIXED> {
     return owns ? f : 0.0;
   }
 
-  // Newton matrix rows: FP64 M = I - gamma J; mixed FP32 W M W^-1
-  __device__ __forceinline__ void assemble(double yv, double rf_d) {
+  // Newton matrix rows: FP64 M = I - gamma J; mixed FP32 W M W^-1 (rf_d =
+  // -gamma, identity); the diagnostic evaluation takes J itself (rf_d = 1, no
+  // identity)
+  __device__ __forceinline__ void assemble(double yv, double rf_d, bool identity = true) {
     const WarpTables &T = A.tab;
     const int G = T.lanes;
     if (owns) xs[tid] = yv;
@@ -313,7 +315,7 @@ struct CtaCell : Core<CtaCell<MIXED>, false, MIXED> {
         MT v = M(tid, j);
         if constexpr (MIXED) v = fmaf(e * cj, sig[j], v);
         else v = fma(e, cj, v);
-        M(tid, j) = rf * v + (tid == j ? MT(1) : MT(0));
+        M(tid, j) = rf * v + ((identity && tid == j) ? MT(1) : MT(0));
       }
     }
   }
@@ -664,6 +666,62 @@ __global__ void __launch_bounds__(256, 1) chem_cta_kernel(const __grid_constant_
   }
 }
 
+// Diagnostic evaluation of the block integrator's RHS (mode 0) or Jacobian
+// with the x_e chain rule (mode 1) on given states: one block per state, the
+// same device code the integrator runs (CtaCell::rhs, CtaCell::assemble), in
+// FP64.  out: mode 0 [nstate][n], mode 1 [nstate][n][n] row-major.
+__global__ void __launch_bounds__(256, 1) eval_cta_kernel(const __grid_constant__ CtaArgs A, int nstate,
+                                                          const double *x, double *out, double *xe_out, int mode,
+                                                          int mat_smem) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const CtaLayout L = cta_layout(A.n, A.nreac, A.tab.nparts, A.G, A.ld, 8, mat_smem != 0);
+  CtaCell<false> c(A, threadIdx.x);
+  const int n = A.n, tid = threadIdx.x;
+  c.kn = A.kn_global + (size_t)blockIdx.x * A.nreac;
+  c.scr = reinterpret_cast<double *>(smem_raw + L.scr);
+  c.xs = reinterpret_cast<double *>(smem_raw + L.xs);
+  c.part = reinterpret_cast<double *>(smem_raw + L.part);
+  c.red_d = reinterpret_cast<double *>(smem_raw + L.red);
+  c.red_k = reinterpret_cast<unsigned long long *>(smem_raw + L.red + 2 * MAXW * 8);
+  c.red_i = reinterpret_cast<int *>(smem_raw + L.red + 2 * MAXW * 16);
+  c.sig = reinterpret_cast<float *>(smem_raw + L.sig);
+  c.perm = reinterpret_cast<int *>(smem_raw + L.perm);
+  c.cols = reinterpret_cast<int *>(smem_raw + L.cols);
+  c.cnt = c.cols + n;
+  c.bsv = reinterpret_cast<double *>(smem_raw + L.bsv);
+  c.ys = reinterpret_cast<double *>(smem_raw + L.ys);
+  c.upan = reinterpret_cast<double *>(smem_raw + L.upan);
+  c.ws = reinterpret_cast<CoefShared *>(smem_raw + L.ws);
+  c.mat = mat_smem ? reinterpret_cast<double *>(smem_raw + L.mat)
+                   : reinterpret_cast<double *>(A.mat_global) + (size_t)blockIdx.x * (n + 2) * A.ld;
+  c.rtol = A.reltol;
+  c.atol = A.abstol;
+  c.cx = (tid < n) ? __ldg(&A.tab.xe_coef[tid]) : 0.0;
+  for (int s = blockIdx.x; s < nstate; s += gridDim.x) {
+    const double n_H = A.density[s];
+    for (int r = tid; r < A.nreac; r += blockDim.x)
+      c.kn[r] = A.rate[(size_t)s * A.nreac + r] * (__ldg(&A.tab.nh_mask[r]) != 0.0 ? n_H : 1.0);
+    if (tid == 0) {
+      c.xs[n + 1] = 1.0;
+      c.part[A.tab.nparts] = 0.0;
+      c.sig[n] = 1.0f;
+      c.sig[n + 1] = 0.0f;
+    }
+    __syncthreads();
+    const double yv = (tid < n) ? x[(size_t)s * n + tid] : 0.0;
+    if (mode == 0) {
+      const double f = c.rhs(yv);
+      if (tid < n) out[(size_t)s * n + tid] = f;
+      if (tid == 0 && xe_out) xe_out[s] = c.xe_last;
+    } else {
+      c.assemble(yv, 1.0, false);
+      __syncthreads();
+      for (int e = tid; e < n * n; e += blockDim.x) out[(size_t)s * n * n + e] = c.M(e / n, e % n);
+    }
+    __syncthreads();
+  }
+}
+
 }  // namespace
 
 // shared memory of one block, and whether the matrix is in it
@@ -692,17 +750,21 @@ size_t chem_cta_global_bytes(const pdr_net *net, bool mixed, int grid) {
   return b;
 }
 
-// The dynamic shared-memory limit of a kernel only ever grows (networks of
-// different sizes share the two kernels), so no call lowers it below what
-// another network's launch needs.
+// The dynamic shared-memory limit of a kernel is set per device and only ever
+// grows there (networks of different sizes share the two kernels), so no call
+// lowers it below what another network's launch needs.
 static cudaError_t ensure_smem_attr(bool mixed, size_t smem) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  dev &= 63;
   static std::mutex mu;
-  static size_t attr[2] = {0, 0};
+  static size_t attr[64][2] = {};
   std::lock_guard<std::mutex> lk(mu);
-  if (smem <= attr[mixed]) return cudaSuccess;
+  if (smem <= attr[dev][mixed]) return cudaSuccess;
   auto k = mixed ? chem_cta_kernel<true> : chem_cta_kernel<false>;
-  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e == cudaSuccess) attr[mixed] = smem;
+  e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess) attr[dev][mixed] = smem;
   return e;
 }
 
@@ -762,4 +824,43 @@ int launch_chem_cta(const pdr_net *net, int ncell, double *ab, const double *rat
   return e == cudaSuccess ? 0 : cuda_fail(e, "chem_cta_kernel launch");
 }
 
+}  // namespace pdr
+
+namespace pdr {
+// Diagnostic launch of eval_cta_kernel (FP64): allocates its per-block scratch
+// (rate constants and, when it does not fit shared memory, the matrix) and
+// frees it after the stream has finished the launch.
+int launch_chem_eval_cta(const pdr_net *net, int nstate, const double *x, const double *rate, const double *dens,
+                         double *out, double *xe_out, int mode, cudaStream_t st) {
+  const WarpTables &T = net->cta;
+  if (!net->cta_ok || T.lanes > 256) return PDR_E_NET;
+  CtaArgs A{};
+  A.tab = T;
+  A.nspec = net->host.nspec;
+  A.nreac = net->host.nreac;
+  A.n = T.neq;
+  A.ld = T.neq | 1;
+  A.G = T.lanes;
+  A.rate = rate;
+  A.density = dens;
+  A.reltol = 1e-8;
+  A.abstol = 1e-30;
+  bool ms = false;
+  const size_t smem = chem_cta_smem(net, false, &ms);
+  const int grid = nstate < 1024 ? nstate : 1024;
+  void *scratch = nullptr;
+  cudaError_t e = cudaMalloc(&scratch, chem_cta_global_bytes(net, false, grid));
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(eval scratch)");
+  A.kn_global = reinterpret_cast<double *>(scratch);
+  A.mat_global = ms ? nullptr : reinterpret_cast<unsigned char *>(scratch) + al16((size_t)grid * T.nreac * 8);
+  e = cudaFuncSetAttribute(eval_cta_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess) {
+    eval_cta_kernel<<<grid, T.lanes, smem, st>>>(A, nstate, x, out, xe_out, mode, ms ? 1 : 0);
+    e = cudaGetLastError();
+  }
+  cudaError_t e2 = cudaStreamSynchronize(st);
+  cudaFree(scratch);
+  if (e != cudaSuccess) return cuda_fail(e, "eval_cta_kernel launch");
+  return e2 == cudaSuccess ? 0 : cuda_fail(e2, "eval_cta_kernel");
+}
 }  // namespace pdr

@@ -78,12 +78,10 @@ extern "C" int pdr_chem_solve_batched_noalloc(const pdr_net *net, int ncell, dou
   pdr_chem_opts o;
   pdr_chem_opts_default(&o);
   if (opts) o = *opts;
-  if (!(o.reltol >= 0.0) || !(o.abstol > 0.0) || o.mxstep <= 0 ||
-      (o.precision != PDR_FP64 && o.precision != PDR_MIXED)) {
-    set_error("pdr_chem_solve_batched_noalloc: invalid options");
-    return PDR_E_ARG;
-  }
-  if (!net->warp_ok || net->host.neq != 32 || o.integrator == 2) {
+  // the same option checks as pdr_chem_solve_batched
+  int rc = check_opts(net, o, "pdr_chem_solve_batched_noalloc");
+  if (rc) return rc;
+  if (!uses_warp_path(net, o)) {
     // the block integrator needs per-block scratch that scales with the grid
     set_error("pdr_chem_solve_batched_noalloc: only the warp integrator (networks of 32 ODE species) "
               "runs without allocation");
@@ -95,7 +93,7 @@ extern "C" int pdr_chem_solve_batched_noalloc(const pdr_net *net, int ncell, dou
   e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceGetAttribute");
   int *scratch = nullptr;
-  int rc = noalloc_scratch(dev, &scratch);
+  rc = noalloc_scratch(dev, &scratch);
   if (rc) return rc;
   cudaStream_t st = (cudaStream_t)stream;
   // the array keeps the previous call's contents: clear the cursors and the redo count
@@ -103,11 +101,12 @@ extern "C" int pdr_chem_solve_batched_noalloc(const pdr_net *net, int ncell, dou
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(no-alloc scratch)");
   int *queue = scratch + 0, *redo_queue = scratch + 1, *redo_count = scratch + 2, *redo = scratch + kCounters;
   const bool mixed = (o.precision == PDR_MIXED);
+  const int sm_use = eff_sms(o, sms);   // opts.max_sms, as pdr_chem_solve_batched applies it
   rc = launch_chem_warp(net, ncell, d_abundance, d_rate, d_density, d_t_end_yr, o, d_status, d_stats, queue,
-                        redo, redo_count, nullptr, nullptr, mixed, sms, st);
+                        redo, redo_count, nullptr, nullptr, mixed, sm_use, st);
   if (rc) return rc;
   if (mixed)
     rc = launch_chem_warp(net, ncell, d_abundance, d_rate, d_density, d_t_end_yr, o, d_status, d_stats,
-                          redo_queue, nullptr, nullptr, redo, redo_count, false, sms, st);
+                          redo_queue, nullptr, nullptr, redo, redo_count, false, sm_use, st);
   return rc;
 }

@@ -499,30 +499,35 @@ int launch_chem_warp(const pdr_net *net, int ncell, double *ab, const double *ra
                                  chem_warp_kernel<32, false, 2>, chem_warp_kernel<32, false, 3>,
                                  chem_warp_kernel<32, true, 0>,  chem_warp_kernel<32, true, 1>,
                                  chem_warp_kernel<32, true, 2>,  chem_warp_kernel<32, true, 3>};
-  // The dynamic shared-memory limit is an attribute of the function: it only
-  // ever grows (to the largest block size used so far), so that a launch with
-  // fewer warps never lowers it below what another block size needs.  The
-  // occupancy is cached per (variant, block size); calls made while a stream
-  // is being captured then issue no attribute changes.
+  // The dynamic shared-memory limit is an attribute of the function on each
+  // device: it only ever grows (to the largest block size used so far on that
+  // device), so that a launch with fewer warps never lowers it below what
+  // another block size needs.  The occupancy is cached per (device, variant,
+  // block size); calls made while a stream is being captured then issue no
+  // attribute changes.
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  dev &= 63;
   static std::mutex mu;
-  static size_t attr_smem[8] = {};
-  static int cached_per_sm[8][9] = {};
-  static size_t cached_smem[8][9] = {};
+  static size_t attr_smem[64][8] = {};
+  static int cached_per_sm[64][8][9] = {};
+  static size_t cached_smem[64][8][9] = {};
   int per_sm = 0;
-  cudaError_t e = cudaSuccess;
   {
     std::lock_guard<std::mutex> lk(mu);
-    if (smem > attr_smem[variant]) {
+    if (smem > attr_smem[dev][variant]) {
       e = cudaFuncSetAttribute(kernels[variant], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute");
-      attr_smem[variant] = smem;
+      attr_smem[dev][variant] = smem;
     }
-    if (cached_smem[variant][wpb] != smem) {
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&cached_per_sm[variant][wpb], kernels[variant], wpb * 32, smem);
+    if (cached_smem[dev][variant][wpb] != smem) {
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&cached_per_sm[dev][variant][wpb], kernels[variant], wpb * 32,
+                                                        smem);
       if (e != cudaSuccess) return cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
-      cached_smem[variant][wpb] = smem;
+      cached_smem[dev][variant][wpb] = smem;
     }
-    per_sm = cached_per_sm[variant][wpb];
+    per_sm = cached_per_sm[dev][variant][wpb];
   }
   if (o.blocks_per_sm > 0 && o.blocks_per_sm < per_sm) per_sm = o.blocks_per_sm;
   if (per_sm < 1) per_sm = 1;

@@ -22,6 +22,7 @@ struct HeatArgs {
   int iE, iH, iH2, iC, iCO, iH2x, iH3x, iH3Ox, iHCOx, iHEx;
   int nr[6];   // NRGR..NRSI, 1-based
   pdr_phys ph;
+  const double *zeta;   // per-cell ZETA (the cosmic-ray variant's zetacrlocal) or null
   const double *density, *Tg, *Td, *uv, *ab, *rate;
   double *out;
 };
@@ -65,7 +66,8 @@ __global__ void __launch_bounds__(256) heating_kernel(const __grid_constant__ He
   const double ncr = 1.0e6 / sqrt(T) /
                      (1.6 * ab[A.iH] * exp(-((400.0 / T) * (400.0 / T))) + 1.4 * ab[A.iH2] * exp(-(18100.0 / (T + 1200.0))));
   const double fuv = (R4(2.2) * EV) * 9.0 * R[A.nr[1]] * ab[A.iH2] * n / (1.0 + ncr / n);
-  const double cr = (R4(9.4) * EV) * (1.3e-17 * A.ph.zeta) * n * ab[A.iH2];
+  const double zeta = A.zeta ? A.zeta[cell] : A.ph.zeta;
+  const double cr = (R4(9.4) * EV) * (1.3e-17 * zeta) * n * ab[A.iH2];
   const double vt = A.ph.v_turb / 1.0e5;
   const double turb = 3.5e-28 * (vt * vt * vt) * (1.0 / 5.0) * n;
   double chem;
@@ -98,7 +100,7 @@ __global__ void __launch_bounds__(256) heating_kernel(const __grid_constant__ He
 
 int launch_heating(const pdr_net *net, int network, const pdr_phys &ph, int ncell, const double *dens,
                    const double *Tg, const double *Td, const double *uv, const double *ab, const double *rate,
-                   double *out, cudaStream_t st) {
+                   const double *zeta, double *out, cudaStream_t st) {
   const HostNet &h = net->host;
   auto idx = [&](const char *a, const char *b) {
     for (int i = 0; i < h.nspec; i++)
@@ -121,7 +123,7 @@ int launch_heating(const pdr_net *net, int network, const pdr_phys &ph, int ncel
   }
   const int maxr = network == 0 ? 240 : 1541;
   if (h.nreac < maxr) { set_error("heating: reaction numbers of the chemical heating exceed the network"); return PDR_E_NET; }
-  A.density = dens; A.Tg = Tg; A.Td = Td; A.uv = uv; A.ab = ab; A.rate = rate; A.out = out;
+  A.density = dens; A.Tg = Tg; A.Td = Td; A.uv = uv; A.ab = ab; A.rate = rate; A.out = out; A.zeta = zeta;
   heating_kernel<<<(ncell + 255) / 256, 256, 0, st>>>(A);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? 0 : cuda_fail(e, "heating_kernel launch");

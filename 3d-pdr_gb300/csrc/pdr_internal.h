@@ -144,4 +144,8 @@ namespace pdr {
 void set_error(const std::string &msg);
 int cuda_fail(cudaError_t e, const char *what);
 int build_device_tables(pdr_net *net);
+// option checks and launch shape shared by the chemistry entry points (capi.cu)
+bool uses_warp_path(const pdr_net *net, const pdr_chem_opts &o);
+int check_opts(const pdr_net *net, const pdr_chem_opts &o, const char *who);
+int eff_sms(const pdr_chem_opts &o, int sms);   // SMs the persistent grid spans
 }  // namespace pdr

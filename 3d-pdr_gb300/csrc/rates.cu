@@ -217,6 +217,7 @@ __global__ void __launch_bounds__(256) rates_kernel(const __grid_constant__ Rate
                                                     const double *__restrict__ rad,
                                                     const double *__restrict__ AV,
                                                     const double *__restrict__ col5,
+                                                    const double *__restrict__ zeta_cell,
                                                     double *__restrict__ rate, int *__restrict__ status) {
   extern __shared__ __align__(16) unsigned char smem[];
   RateRow *tab = reinterpret_cast<RateRow *>(smem);
@@ -236,6 +237,8 @@ __global__ void __launch_bounds__(256) rates_kernel(const __grid_constant__ Rate
   const double dopw = ph.v_turb / (1000.0 * 1.0e-8), radw = 8.0e7;
   for (int cell = blockIdx.x * wpb + (threadIdx.x >> 5); cell < ncell; cell += gridDim.x * wpb) {
     const double t = Tg[cell], td = Td[cell];
+    // ZETA, or the cell's own rate in the cosmic-ray variant (zetacrlocal)
+    const double zeta = zeta_cell ? zeta_cell[cell] : ph.zeta;
     const double *rs = rad + (size_t)cell * nrays;
     const double *av = AV + (size_t)cell * nrays;
     const double *cc = col5 + (size_t)cell * nrays * 5;
@@ -285,15 +288,15 @@ __global__ void __launch_bounds__(256) rates_kernel(const __grid_constant__ Rate
           case RK_PHOTO:
             for (int ray = 0; ray < nrays; ray++) k = k + a * rs[ray] * exp(-(g * av[ray])) / 2.0;
             break;
-          case RK_CRP: k = a * ph.zeta; break;
-          case RK_CRPHOT: k = a * ph.zeta * pow(t / 300.0, b) * g / (1.0 - ph.omega); break;
+          case RK_CRP: k = a * zeta; break;
+          case RK_CRPHOT: k = a * zeta * pow(t / 300.0, b) * g / (1.0 - ph.omega); break;
           case RK_FREEZE:
           case RK_ELFRZE: {
             const double cion = (b == 0.0) ? 1.0 : (b == 1.0 ? 1.0 + 16.71e-4 / (ph.grain_radius * t) : 0.0);
             k = a * 4.57e4 * 2.4e-22 * sqrt(t / g) * cion * 0.3;
             break;
           }
-          case RK_CRH: k = 2.06e-3 * ph.zeta * 2.4e-22 * ((g <= 1210.0) ? 1.0e5 : 0.0); break;
+          case RK_CRH: k = 2.06e-3 * zeta * 2.4e-22 * ((g <= 1210.0) ? 1.0e5 : 0.0); break;
           case RK_PHOTD: {
             const double y = (t < 50.0) ? 3.5e-3 : (t < 85.0 ? 4.0e-3 : (t < 100.0 ? 5.5e-3 : 7.5e-3));
             for (int ray = 0; ray < nrays; ray++) k = k + 1.7e8 * rs[ray] * exp(-(1.8 * av[ray])) * 2.4e-22 * y;
@@ -321,21 +324,25 @@ __global__ void __launch_bounds__(256) rates_kernel(const __grid_constant__ Rate
 }  // namespace
 
 int launch_rates(const pdr_net *net, const pdr_phys &ph, int ncell, int nrays, const double *T,
-                 const double *Td, const double *rad, const double *AV, const double *col5, double *rate,
-                 int *status, int sm_count, cudaStream_t st) {
+                 const double *Td, const double *rad, const double *AV, const double *col5, const double *zeta,
+                 double *rate, int *status, int sm_count, cudaStream_t st) {
   const size_t smem = sizeof(RateRow) * (size_t)net->rates.nreac;
   if (smem > 200 * 1024) return PDR_E_NET;
   // the attribute only grows, so concurrent launches for networks of
   // different sizes (server lanes) never lower it under each other
-  cudaError_t e = cudaSuccess;
+  // (per device: the attribute is a property of the function on each device)
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  dev &= 63;
   {
     static std::mutex mu;
-    static size_t attr = 0;
+    static size_t attr[64] = {};
     std::lock_guard<std::mutex> lk(mu);
-    if (smem > attr) {
+    if (smem > attr[dev]) {
       e = cudaFuncSetAttribute(rates_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(rates)");
-      attr = smem;
+      attr[dev] = smem;
     }
   }
   int per_sm = 0;
@@ -345,7 +352,8 @@ int launch_rates(const pdr_net *net, const pdr_phys &ph, int ncell, int nrays, c
   long long cap = (long long)sm_count * per_sm;
   if (blocks > cap) blocks = cap;
   if (blocks < 1) blocks = 1;
-  rates_kernel<<<(int)blocks, 256, smem, st>>>(net->rates, ph, ncell, nrays, T, Td, rad, AV, col5, rate, status);
+  rates_kernel<<<(int)blocks, 256, smem, st>>>(net->rates, ph, ncell, nrays, T, Td, rad, AV, col5, zeta, rate,
+                                                status);
   e = cudaGetLastError();
   return e == cudaSuccess ? 0 : cuda_fail(e, "rates_kernel launch");
 }

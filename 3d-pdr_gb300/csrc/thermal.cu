@@ -136,6 +136,7 @@ __global__ void __launch_bounds__(256) thermal_kernel(const __grid_constant__ Th
 
 struct LevConvArgs {
   int ncell, ncool, nspec, vec;
+  int copy;   // copy SOLUTION into the populations in the same sweep
   int nlev[PDR_MAX_COOLANTS], species[PDR_MAX_COOLANTS];
   float inv_nlev[PDR_MAX_COOLANTS];
   const double *sol[PDR_MAX_COOLANTS];
@@ -238,7 +239,7 @@ __global__ void __launch_bounds__(LC_CELLS) levconv_kernel(const __grid_constant
             const int cb = __float2int_rz(__fmul_rn(__int2float_rn(eb) + 0.5f, inv));
             if (level_moved(sv[u].x, pv[u].x, floor_of[k][ca])) bad[k][ca] = 1;
             if (level_moved(sv[u].y, pv[u].y, floor_of[k][cb])) bad[k][cb] = 1;
-            p2[q] = sv[u];   // 3DPDR.F90:1212-1229
+            if (A.copy) p2[q] = sv[u];   // 3DPDR.F90:1212-1229
           }
         }
       }
@@ -248,7 +249,7 @@ __global__ void __launch_bounds__(LC_CELLS) levconv_kernel(const __grid_constant
       const int cl = __float2int_rz(__fmul_rn(__int2float_rn(e) + 0.5f, inv));
       const double sv = s[e];
       if (level_moved(sv, p[e], floor_of[k][cl])) bad[k][cl] = 1;
-      p[e] = sv;
+      if (A.copy) p[e] = sv;
     }
   }
   __syncthreads();
@@ -274,6 +275,30 @@ __global__ void __launch_bounds__(256) levconv_reset_kernel(int ncell, const int
   if (counts[0] != ncell) return;
   for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ncell; c += gridDim.x * blockDim.x)
     flags[c] &= (unsigned char)~LCONV;
+}
+
+// Without thermal balance the reference updates the populations only while
+// some cell has not converged: once every cell has, it leaves the loop before
+// the update (3DPDR.F90:1161-1172, goto 2) and keeps the previous populations.
+// The decision needs the count over all cells, so this pass runs after the
+// check and copies SOLUTION into the populations unless counts[0] == ncell.
+__global__ void __launch_bounds__(256) levconv_copy_kernel(const __grid_constant__ LevConvArgs A) {
+  if (A.counts[0] == A.ncell) return;
+  for (int k = 0; k < A.ncool; k++) {
+    const size_t ne = (size_t)A.ncell * A.nlev[k];
+    const double *s = A.sol[k];
+    double *p = A.pop[k];
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    if (A.vec) {
+      const size_t npair = ne >> 1;
+      const double2 *s2 = reinterpret_cast<const double2 *>(s);
+      double2 *p2 = reinterpret_cast<double2 *>(p);
+      for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < npair; q += stride) p2[q] = s2[q];
+      if ((ne & 1) && blockIdx.x == 0 && threadIdx.x == 0) p[ne - 1] = s[ne - 1];
+    } else {
+      for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < ne; e += stride) p[e] = s[e];
+    }
+  }
 }
 
 }  // namespace
@@ -332,16 +357,21 @@ int launch_level_convergence(int ncell, int ncool, const int *nlev, const double
   A.flags = flags;
   A.cconv = cconv;
   A.counts = counts;
+  A.copy = thermal_balance ? 1 : 0;
   cudaError_t e = cudaMemsetAsync(counts, 0, sizeof(int) * (1 + ncool), st);
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(level convergence counts)");
   levconv_kernel<<<(ncell + LC_CELLS - 1) / LC_CELLS, LC_CELLS, 0, st>>>(A);
   e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "levconv_kernel launch");
+  const int blocks = std::max(1, std::min((ncell + 255) / 256, sm_count * 8));
   if (thermal_balance) {
-    const int blocks = std::max(1, std::min((ncell + 255) / 256, sm_count * 8));
     levconv_reset_kernel<<<blocks, 256, 0, st>>>(ncell, counts, flags);
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "levconv_reset_kernel launch");
+  } else {
+    levconv_copy_kernel<<<blocks, 256, 0, st>>>(A);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "levconv_copy_kernel launch");
   }
   return 0;
 }

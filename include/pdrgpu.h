@@ -204,6 +204,14 @@ int pdr_rates_batched(const pdr_net *net, const pdr_phys *phys, int ncell, int n
                       const double *d_T, const double *d_Td, const double *d_rad_surface,
                       const double *d_AV, const double *d_column5, double *d_rate, int *d_status,
                       void *stream);
+/* The cosmic-ray variant of the same call (3dpdr_cr.tgz: calc_reac_rates.F90:19,
+ * 40,254-303,359-361 take zetacrlocal in place of ZETA): d_zeta[ncell] is each
+ * cell's cosmic-ray rate in the units of pdr_phys.zeta (s^-1 / 1.3e-17), used by
+ * the CRP, CRPHOT and cosmic-ray desorption branches; NULL takes phys->zeta. */
+int pdr_rates_batched_cr(const pdr_net *net, const pdr_phys *phys, int ncell, int nrays,
+                         const double *d_T, const double *d_Td, const double *d_rad_surface,
+                         const double *d_AV, const double *d_column5, const double *d_zeta,
+                         double *d_rate, int *d_status, void *stream);
 /* special reaction numbers NRGR, NRH2, NRHD, NRCO, NRCI, NRSI (1-based, 0 = absent) */
 int pdr_net_special_reactions(const pdr_net *net, int nr[6]);
 
@@ -300,6 +308,13 @@ int pdr_heating_batched(const pdr_net *net, int network, const pdr_phys *phys, i
                         const double *d_density, const double *d_Tgas, const double *d_Tdust,
                         const double *d_uv_field, const double *d_abundance, const double *d_rate,
                         double *d_heating, void *stream);
+/* The cosmic-ray variant (3dpdr_cr.tgz sub_calculate_heating.F90:11,26,210): the
+ * cosmic-ray heating term takes each cell's d_zeta[ncell] (units of
+ * pdr_phys.zeta) in place of ZETA; NULL takes phys->zeta. */
+int pdr_heating_batched_cr(const pdr_net *net, int network, const pdr_phys *phys, int ncell,
+                           const double *d_density, const double *d_Tgas, const double *d_Tdust,
+                           const double *d_uv_field, const double *d_abundance, const double *d_rate,
+                           const double *d_zeta, double *d_heating, void *stream);
 
 /* ---- outer-iteration controllers resident on the device ----
  * The per-cell state of the thermal-balance search (3DPDR.F90:928-1050) lives
@@ -346,7 +361,14 @@ int pdr_thermal_balance_batched(const pdr_thermal_params *params, int level_conv
  * for ncool (<= PDR_MAX_COOLANTS) coolants: host arrays nlev[k], species[k]
  * (the coolant's species, NCx NC NO NCO; nlev <= 4096) and of device pointers
  * d_solution[k][ncell*nlev[k]] (the new populations) and d_pop[k] (the
- * current ones, overwritten with the new).  A level is checked when its new
+ * current ones, overwritten with the new).  Both are indexed [cell][level]:
+ * element (c, l) is at c*nlev[k] + l.  The reference's CII_SOLUTION(pp,ilevel)
+ * is column-major, i.e. [level][cell] in memory, so a Fortran caller passes
+ * arrays dimensioned (nlev, ncell) or transposes SOLUTION first.  The
+ * populations are replaced by SOLUTION in every cell, except that without
+ * thermal balance and with every cell converged they are kept, as the
+ * reference leaves its loop before the update then (3DPDR.F90:1161-1172).
+ * A level is checked when its new
  * population is >= 1e-10 * abundance(species); the coolant converged in a cell
  * when every checked level changed by a relative 2|s-p|/(s+p) <= 1e-2.  Sets
  * PDR_TB_LEVEL_CONVERGED in d_flags where all coolants converged; with
@@ -364,7 +386,11 @@ int pdr_level_convergence_batched(int ncell, int ncool, const int *nlev, const d
  * it (mode 0: d_out[nstate*neq], x_e of each state in d_xe), or the analytic
  * Jacobian including dx_e/dx_j (mode 1: d_out[nstate*neq*neq], row-major
  * J[i][j] = df_i/dx_j; jacobian_<net>.c is the reference counterpart, without
- * the x_e chain rule).  d_x[nstate*neq], d_rate[nstate*nreac], d_density[nstate]. */
+ * the x_e chain rule).  d_x[nstate*neq], d_rate[nstate*nreac], d_density[nstate].
+ * Modes 0 and 1 run the code of the integrator the network uses (one warp per
+ * cell for 32 ODE species, else one block per cell); modes 2 and 3 are modes
+ * 0 and 1 through the block integrator's code for any network.  Modes 2 and 3
+ * allocate temporary scratch and synchronise the stream. */
 int pdr_chem_eval_batched(const pdr_net *net, int nstate, const double *d_x, const double *d_rate,
                           const double *d_density, int mode, double *d_out, double *d_xe, void *stream);
 /* second derivatives of the shielding splines: XLAMBDA's 30-point table

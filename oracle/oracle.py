@@ -200,7 +200,19 @@ class Network:
                                             _ptr(stats, _lp) if want_stats else None)
         return (ab, st, stats) if want_stats else (ab, st)
 
-    def rates(self, phys, T, Td, rad_surface, AV, column5, nthreads=0):
+    def rates(self, phys, T, Td, rad_surface, AV, column5, nthreads=0, zeta=None):
+        """zeta (ncell,) or None: per-cell ZETA of the cosmic-ray variant
+        (calc_reac_rates.F90 of 3dpdr_cr.tgz takes zetacrlocal in place of ZETA)."""
+        if zeta is not None:
+            out = np.zeros((len(T), self.nreac))
+            st = 0
+            for c in range(len(T)):
+                ph = OrcPhys(float(zeta[c]), phys.omega, phys.grain_radius, phys.metallicity, phys.g2d,
+                             phys.v_turb, phys.h2form, phys.xlambda_linear)
+                out[c:c + 1], s = self.rates(ph, T[c:c + 1], Td[c:c + 1], rad_surface[c:c + 1], AV[c:c + 1],
+                                             column5[c:c + 1], nthreads=1)
+                st = st or s
+            return out, st
         T = np.ascontiguousarray(T, dtype=np.float64)
         ncell = T.shape[0]
         nrays = rad_surface.shape[1]

@@ -151,6 +151,9 @@ void orc_level_convergence(int ncell, int ncool, const int *nlev, const double *
   /* :1202-1206: with thermal balance every level_converged is reset once all cells converged */
   if (thermal_balance && counts[0] == ncell)
     for (int c = 0; c < ncell; c++) flags[c] &= (unsigned char)~LCONV;
+  /* :1161-1172: without thermal balance, once every cell converged the
+   * reference leaves the loop (goto 2) before the population update */
+  if (!thermal_balance && counts[0] == ncell) return;
   for (int k = 0; k < ncool; k++)                                    /* :1212-1229 */
     for (long long e = 0; e < (long long)ncell * nlev[k]; e++) pop[k][e] = solution[k][e];
 }

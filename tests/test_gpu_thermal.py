@@ -163,6 +163,35 @@ def test_all_converged_resets_level_flags_on_device(cuda):
     assert np.all(tb.flags.cpu().numpy() == G.TB_LEVEL_CONVERGED)
 
 
+@pytest.mark.parametrize("offset", [0, 1])
+def test_all_converged_without_thermal_balance_keeps_the_populations(cuda, offset):
+    """3DPDR.F90:1161-1172: without thermal balance, once every cell converged
+    the populations are not replaced by SOLUTION (levels below the 1e-10 floor
+    may differ by any amount); with one cell unconverged all are replaced."""
+    import torch
+    rng = np.random.default_rng(31)
+    n = 1001
+    s = np.abs(rng.normal(size=(n, 41))) + 0.1
+    s[:, 40] = 1e-13                      # below the floor 1e-10 * abundance
+    p = s.copy()
+    p[:, 40] = 7e-12                      # differs, but is never checked
+    ab = np.ones((n, 3))
+    for thermal_balance, unconverged in ((False, False), (True, False), (False, True)):
+        pp = p.copy()
+        if unconverged:
+            pp[n // 2, 3] *= 1.5
+        tb = G.ThermalBalance(torch.zeros(n, dtype=torch.float64, device=cuda))
+        dp = dev_offset(pp, cuda, offset)
+        counts = tb.level_convergence([dev_offset(s, cuda, offset)], [dp], dev(ab, cuda), [1],
+                                      thermal_balance=thermal_balance)
+        want = pp.copy()
+        flags = np.zeros(n, dtype=np.uint8)
+        _, counts_r = O.level_convergence([s], [want], ab, [1], flags, thermal_balance)
+        assert np.array_equal(counts.cpu().numpy(), counts_r)
+        assert np.array_equal(dp.cpu().numpy(), want)
+        assert np.array_equal(want, pp if not (thermal_balance or unconverged) else s)
+
+
 def test_device_heating_and_cooling_feed_the_update(cuda):
     """The rates -> heating -> (levpop cooling) -> thermal update chain with
     every array on the device; the oracle update on the same heating and

@@ -266,6 +266,33 @@ def test_level_convergence_rules():
     assert list(flags) == [LCONV, LCONV]
 
 
+def test_all_converged_without_thermal_balance_keeps_the_populations():
+    """Without THERMALBALANCE the reference leaves the loop once every cell
+    converged (3DPDR.F90:1161-1172, goto 2) and skips the update of
+    :1212-1229: the previous populations are kept, also on levels below the
+    floor whose SOLUTION differs from them by any amount.  While one cell has
+    not converged every cell's populations are replaced."""
+    sol = np.array([[1.0, 0.0, 1e-11, 2.0], [1.0, 1.0, 1.0, 1.0]])
+    pop = np.array([[1.0, 0.0, 5.0, 2.0], [1.0, 1.0, 1.0, 1.005]])
+    ab = np.ones((2, 2))
+    p = pop.copy()
+    flags = np.zeros(2, dtype=np.uint8)
+    cconv, counts = O.level_convergence([sol], [p], ab, [0], flags, False)
+    assert list(counts) == [2, 2] and list(flags) == [LCONV, LCONV]
+    assert np.array_equal(p, pop)
+    # with thermal balance the reference still updates (goto 1)
+    p = pop.copy()
+    O.level_convergence([sol], [p], ab, [0], np.zeros(2, dtype=np.uint8), True)
+    assert np.array_equal(p, sol)
+    # one cell not converged: every cell is updated
+    sol2 = np.vstack([sol, [[1.0, 2.0, 1.0, 1.0]]])
+    pop2 = np.vstack([pop, [[1.0, 1.0, 1.0, 1.0]]])
+    p = pop2.copy()
+    cconv, counts = O.level_convergence([sol2], [p], np.ones((3, 2)), [0], np.zeros(3, dtype=np.uint8), False)
+    assert list(counts) == [2, 2]
+    assert np.array_equal(p, sol2)
+
+
 def test_level_convergence_needs_every_coolant():
     rng = np.random.default_rng(3)
     n = 50

@@ -82,3 +82,41 @@ def test_noalloc_rejects_more_cells_than_its_scratch():
                                             C.byref(G.chem_opts("mixed")), _vp(st), None, None)
     assert rc == -1001
     assert b"262144" in lib.pdr_last_error()
+
+
+def test_noalloc_takes_the_batched_entry_points_options():
+    """The same option checks as pdr_chem_solve_batched (an integrator outside
+    0..2 is refused by both), and the same SM limit: with max_sms set, both
+    give the same result bit for bit."""
+    import torch
+    dev = torch.device("cuda:0")
+    net = G.Network("reduced")
+    lib = G.lib()
+    lib.pdr_chem_solve_batched_noalloc.argtypes = [C.c_void_p, C.c_int] + [C.c_void_p] * 4 + \
+        [C.POINTER(G.ChemOpts), C.c_void_p, C.c_void_p, C.c_void_p]
+    w = W.chemistry("C1", ncell=16)
+    onet = O.Network("reduced")
+    rates, _ = onet.rates(O.phys(w.zeta, w.omega, w.grain_radius, w.metallicity, w.g2d, w.v_turb_kms),
+                          w.T, w.Td, w.rad_surface, w.AV, w.column5)
+    ab0 = np.tile(W.initial_abundances(onet.species, s_plus=False), (w.ncell, 1))
+    rate = torch.as_tensor(rates, device=dev)
+    dens = torch.as_tensor(w.n_H, device=dev)
+    st = torch.zeros(w.ncell, dtype=torch.int32, device=dev)
+    bad = G.chem_opts("mixed")
+    bad.integrator = 7
+    ab = torch.as_tensor(ab0, device=dev).clone()
+    for fn in (lib.pdr_chem_solve_batched, lib.pdr_chem_solve_batched_noalloc):
+        assert fn(net.handle, w.ncell, _vp(ab), _vp(rate), _vp(dens), None, C.byref(bad), _vp(st), None,
+                  None) == -1001
+    opts = G.chem_opts("mixed")
+    opts.max_sms = 8
+    out = []
+    for fn in (lib.pdr_chem_solve_batched, lib.pdr_chem_solve_batched_noalloc):
+        ab = torch.as_tensor(ab0, device=dev).clone()
+        rc = fn(net.handle, w.ncell, _vp(ab), _vp(rate), _vp(dens), None, C.byref(opts), _vp(st), None,
+                C.c_void_p(torch.cuda.current_stream().cuda_stream))
+        assert rc == 0, lib.pdr_last_error()
+        torch.cuda.synchronize()
+        assert (st.cpu().numpy() == 0).all()
+        out.append(ab.cpu().numpy())
+    assert np.array_equal(out[0], out[1])
