@@ -62,12 +62,24 @@ def build_test_driver():
     return exe
 
 
-def build_oracle(ref_dir="/root/reference"):
+def reference_dir():
+    """The 3D-PDR source tree, for the reference's own network code: the
+    PDR_REFERENCE environment variable, else the tree mounted beside this
+    build (absent on machines that only run the prebuilt library)."""
+    d = os.environ.get("PDR_REFERENCE") or "/root/reference"
+    return d if os.path.exists(os.path.join(d, "odes_reduced.c")) else None
+
+
+def build_oracle(ref_dir=None):
+    """liboracle.so (-O2) and liboracle_O0.so (-O0, the optimisation level the
+    reference compiles its C with, makefile:139-145), plus the reference's
+    generated network code (oracle/_ref) when its sources are present."""
     oracle = os.path.join(ROOT, "oracle")
     r = subprocess.run(["make", "-s", "-C", oracle, "all"], capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"oracle build failed:\n{r.stderr}")
-    if os.path.isdir(ref_dir) and os.path.exists(os.path.join(ref_dir, "odes_reduced.c")):
+    ref_dir = ref_dir or reference_dir()
+    if ref_dir:
         r = subprocess.run(["make", "-s", "-C", oracle, "ref", f"REF={ref_dir}"], capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"reference objects build failed:\n{r.stderr}")

@@ -13,6 +13,8 @@
 //   bool owns; bool leader();  void sync();
 //   double sum_all(double); float sum_all(float); double max_all(double);
 //   double rhs(double y_own);  bool setup(double y_own);  double solve(double b_own);
+//   and, for the mixed form, double solve32(double b_own, float gscale, float &x32)
+//   (the correction times gscale, in FP64 and in FP32);
 // Norms are kept squared (the tests compare squares, no sqrt); the step-ratio
 // heuristics eta = 1/((bias*e)^(1/k) + 1e-6) are evaluated in FP32.
 #pragma once
@@ -166,9 +168,20 @@ struct Core {
     const NT t = self().owns ? (NT)v * ewt : NT(0);
     return self().sum_all(t * t) * (NT)self().inv_n;
   }
+  // the same norm of a value already held in FP32 (the mixed form's Newton
+  // correction comes out of the FP32 solve): no conversion
+  __device__ __forceinline__ float wrms2_32(float v) {
+    const float t = self().owns ? v * ewt : 0.0f;
+    return self().sum_all(t * t) * (float)self().inv_n;
+  }
+
+  // FP32 copies of the tolerances (mixed form), set at the start of integrate()
+  float rtol32 = 0.0f, atol32 = 0.0f;
 
   __device__ __forceinline__ void set_ewt() {
-    if constexpr (NORM32) ewt = self().owns ? __frcp_rn((float)(rtol * fabs(z[0]) + atol)) : 0.0f;
+    // mixed: the weight is FP32, so it is formed from the FP32 value of y (one
+    // conversion instead of an FP64 FMA and a conversion)
+    if constexpr (NORM32) ewt = self().owns ? __frcp_rn(fmaf(rtol32, fabsf((float)z[0]), atol32)) : 0.0f;
     else ewt = self().owns ? rcp_nr(rtol * fabs(z[0]) + atol) : 0.0;
   }
 
@@ -434,10 +447,19 @@ struct Core {
       const double rz1 = rl1 * z[1];   // fixed during the iteration
       for (;;) {
         tmp = gamma * ftmp - (rz1 + acor);
-        tmp = self().solve(tmp);
-        if (gscale != NT(1)) tmp *= (double)gscale;
+        NT del2;
+        if constexpr (NORM32) {
+          // the FP32 solve returns the correction already scaled by gscale,
+          // and its FP32 value feeds the norm
+          float t32;
+          tmp = self().solve32(tmp, gscale, t32);
+          del2 = wrms2_32(t32);
+        } else {
+          tmp = self().solve(tmp);
+          if (gscale != NT(1)) tmp *= (double)gscale;
+          del2 = wrms2(tmp);
+        }
         nni++;
-        const NT del2 = wrms2(tmp);
         acor += tmp;
         y = z[0] + acor;
         if (mcor > 0) crate2 = fmax(NT(CRDOWN * CRDOWN) * crate2, del2 / delp2);
@@ -681,6 +703,8 @@ struct Core {
       for (int j = 0; j < 6; j++) { ws->tqd[j] = 0.0; ws->tqf[j] = 0.0f; }
     }
     self().sync();
+    rtol32 = (float)rtol;
+    atol32 = (float)atol;
     nfe = nje = nsetups = nni = ncfn = netf = 0;
     nst = nstlp = 0;
     saved_tq5 = NT(0);

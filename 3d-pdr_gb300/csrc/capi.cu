@@ -27,7 +27,7 @@ extern int global_module_mp_nelect_ __attribute__((weak));
 
 namespace pdr {
 
-size_t chem_warp_smem_per_warp(int nsp, int nreac, int nparts, bool mixed, bool zshared);
+size_t chem_warp_smem_per_warp(const WarpTables &T, bool mixed, bool zshared);
 int launch_chem_warp(const pdr_net *net, int ncell, double *ab, const double *rate, const double *dens,
                      const double *tend, const pdr_chem_opts &o, int *status, int *stats, int *queue,
                      int *fb_list, int *fb_count, const int *cell_list, const int *total_ptr, bool mixed,

@@ -70,7 +70,7 @@ struct CtaArgs {
   int *fallback_list;
   int *fallback_count;
   int refill_static;
-  double *kn_global;      // [gridDim.x][nreac] rate constants (times n_H where the RHS has it)
+  double *kn_global;      // [gridDim.x][tab.nkn + 1] rate constants (times n_H where the RHS has it)
   void *mat_global;       // [gridDim.x][(n+2)*ld] Newton matrix, when it is not in shared memory
 };
 
@@ -81,16 +81,18 @@ struct CtaLayout {
 
 __host__ __device__ inline size_t al16(size_t x) { return (x + 15) & ~size_t(15); }
 
-__host__ __device__ inline CtaLayout cta_layout(int n, int nreac, int nparts, int G, int ld, size_t mt,
-                                                bool mat_smem) {
+__host__ __device__ inline CtaLayout cta_layout(const WarpTables &T, int ld, size_t mt, bool mat_smem) {
+  const int n = T.neq, nreac = T.nreac, nparts = T.nparts, G = T.lanes;
   CtaLayout L;
   size_t o = 0;
-  const size_t scr = (size_t)nreac * (8 > 2 * mt ? 8 : 2 * mt);
+  // scr: the RHS operands (FP64) or the two Jacobian scatter buffers
+  size_t scr = (size_t)nreac * (8 > 2 * mt ? 8 : 2 * mt);
+  if (8 * (size_t)T.nop > scr) scr = 8 * (size_t)T.nop;
   L.scr = o; o += al16(scr);
   L.xs = o; o += al16(8 * (size_t)(n + 2));
   L.part = o; o += al16(8 * (size_t)(nparts + 1));
   L.red = o; o += al16(2 * MAXW * (8 + 8 + 4));   // sums, argmax keys, argmax rows
-  L.sig = o; o += al16(4 * (size_t)(n + 2));
+  L.sig = o; o += al16(4 * (size_t)(n + 2) * 2);   // column scales, then the FP32 slot values
   L.perm = o; o += al16(4 * (size_t)n);
   L.cols = o; o += al16(4 * (size_t)(n + MAXW));   // nonzero U columns of a panel, per-warp counts
   L.bsv = o; o += al16(mt * (size_t)G);
@@ -140,13 +142,14 @@ struct CtaCell : Core<CtaCell<MIXED>, false, MIXED> {
   unsigned long long *red_k;  // [2][MAXW] argmax keys
   int *red_i;            // [2][MAXW] argmax rows
   float *sig;
+  float *xs32;           // [n+2] FP32 copy of the slot values at setup (mixed)
   int *perm;
   int *cols, *cnt;       // nonzero columns of the current U panel; per-warp counts
   MT *bsv, *ys, *upan, *mat;
   int rbuf = 0;          // alternating reduction buffer
   double cx;
   int mystep;
-  double wsc, ssc;
+  float wsc32, ssc32;    // mixed form: setup-time weight and its inverse (FP32 matrix scaling)
 
   __device__ __forceinline__ CtaCell(const CtaArgs &a, int t)
       : A(a), tid(t), lane(t & 31), warp(t >> 5), nw(blockDim.x >> 5), n(a.n), ld(a.ld), owns(t < a.n),
@@ -211,26 +214,50 @@ struct CtaCell : Core<CtaCell<MIXED>, false, MIXED> {
 
   __device__ __forceinline__ double slot_value(int s, double xe) const { return s == n ? xe : xs[s]; }
 
-  // f(y): returns f of this thread's species, records x_e of this call
+  // per-cell rate constants (kn_r = k_r, times n_H for the terms that carry
+  // it), the extras |nu| kn_r of the RHS terms with |nu| > 1 and a zero for
+  // the padding terms
+  __device__ __forceinline__ void load_rates(const double *rate, double n_H) {
+    const WarpTables &T = A.tab;
+    for (int r = tid; r < T.nreac; r += blockDim.x)
+      kn[r] = __ldg(&rate[r]) * (__ldg(&T.nh_mask[r]) != 0.0 ? n_H : 1.0);
+    if (tid == 0) kn[T.nkn] = 0.0;
+    __syncthreads();
+    for (int e = tid; e < T.nkext; e += blockDim.x) {
+      const int2 q = __ldg(&T.kext[e]);
+      kn[T.nreac + e] = (double)q.y * kn[q.x];
+    }
+  }
+
+  // f(y): returns f of this thread's species, records x_e of this call.  The
+  // operands are the slot values and the products x_a x_b of the two-body
+  // reactant pairs; each stoichiometric term is one FMA with the signed rate
+  // constant (the warp integrator's scheme, stride G).
   __device__ __forceinline__ double rhs(double yv) {
     const WarpTables &T = A.tab;
     const int G = T.lanes;
-    if (owns) xs[tid] = yv;
+    double *P = scr;
+    if (owns) P[tid] = yv;
     const double xe = sum_all(owns ? cx * yv : 0.0);
     this->xe_last = xe;
+    if (tid == 0) {
+      P[n] = xe;
+      P[n + 1] = 1.0;
+    }
 #pragma unroll 4
-    for (int r = tid; r < T.nreac; r += G) {
-      const int2 ab = __ldg(&T.rab[r]);
-      scr[r] = kn[r] * slot_value(ab.x, xe) * slot_value(ab.y, xe);
+    for (int p = tid; p < T.npairs; p += G) {
+      const int2 ab = __ldg(&T.pairs[p]);
+      P[n + 2 + p] = (ab.x == n ? xe : P[ab.x]) * (ab.y == n ? xe : P[ab.y]);
     }
     __syncthreads();
     double s = 0.0;
 #pragma unroll 4
     for (int t = 0; t < T.rhs_len; t++) {
-      const int rf = __ldg(&T.rhs_rf[t * G + tid]);
-      const double nu = __ldg(&T.rhs_nu[t * G + tid]);
-      s = fma(nu, scr[rf & 0xffff], s);
-      const int fl = (rf >> 16) - 1;
+      const int2 d = __ldg(&T.rhs_t[t * G + tid]);
+      const double k = kn[d.x & 0xffff];
+      const double ks = __hiloint2double(__double2hiint(k) ^ (d.y & (int)0x80000000u), __double2loint(k));
+      s = fma(ks, P[d.y & 0x7fffffff], s);
+      const int fl = (int)((unsigned)d.x >> 16) - 1;
       if (fl >= 0) { part[fl] = s; s = 0.0; }
     }
     __syncthreads();
@@ -249,21 +276,30 @@ struct CtaCell : Core<CtaCell<MIXED>, false, MIXED> {
     const int G = T.lanes;
     if (owns) xs[tid] = yv;
     if constexpr (MIXED) {
-      ssc = this->rtol * fabs(yv) + this->atol;
-      wsc = 1.0 / ssc;
-      if (owns) sig[tid] = (float)(ssc / this->atol);
+      // column scales rtol|y|+atol normalised by atol, formed in FP32 from the
+      // FP32 value of y (the matrix is FP32)
+      const float y32 = (float)yv;
+      ssc32 = fmaf(this->rtol32, fabsf(y32), this->atol32);
+      wsc32 = __frcp_rn(ssc32);
+      if (owns) {
+        sig[tid] = ssc32 * __frcp_rn(this->atol32);
+        xs32[tid] = y32;
+      }
     }
     const double xe = sum_all(owns ? cx * yv : 0.0);
     MT *Da = reinterpret_cast<MT *>(scr);
     MT *Db = Da + T.nreac;
+    const float xe32 = MIXED ? (float)xe : 0.0f;
 #pragma unroll 4
     for (int r = tid; r < T.nreac; r += G) {
       const int2 ab = __ldg(&T.rab[r]);
-      const double k = kn[r];
       if constexpr (MIXED) {
-        Da[r] = (float)(k * slot_value(ab.y, xe)) * sig[ab.x];
-        Db[r] = (float)(k * slot_value(ab.x, xe)) * sig[ab.y];
+        // one conversion of the rate constant per reaction, the rest in FP32
+        const float k32 = (float)kn[r];
+        Da[r] = k32 * ((ab.y == n ? xe32 : xs32[ab.y]) * sig[ab.x]);
+        Db[r] = k32 * ((ab.x == n ? xe32 : xs32[ab.x]) * sig[ab.y]);
       } else {
+        const double k = kn[r];
         Da[r] = k * slot_value(ab.y, xe);
         Db[r] = (ab.y == n + 1) ? 0.0 : k * slot_value(ab.x, xe);
       }
@@ -308,7 +344,7 @@ struct CtaCell : Core<CtaCell<MIXED>, false, MIXED> {
     if (owns) {
       const MT e = M(tid, n);
       MT rf;
-      if constexpr (MIXED) rf = (MT)(rf_d * (wsc * this->atol));
+      if constexpr (MIXED) rf = (MT)rf_d * (wsc32 * this->atol32);
       else rf = (MT)rf_d;
       for (int j = 0; j < n; j++) {
         const MT cj = (MT)__ldg(&T.xe_coef[j]);
@@ -508,12 +544,25 @@ struct CtaCell : Core<CtaCell<MIXED>, false, MIXED> {
     return ok;
   }
 
-  // x = M^-1 b for this thread's component
+  // x = M^-1 b for this thread's component (FP64 form)
   __device__ __forceinline__ double solve(double b) {
+    const MT xv = lin_solve(owns ? (MT)b : MT(0));
+    return owns ? (double)xv : 0.0;
+  }
+
+  // mixed form: the residual converted once and scaled in FP32 (the scaling
+  // of the FP32 matrix); the correction comes back times ssc*gscale, in FP32
+  // for the norm and in FP64 for the state
+  __device__ __forceinline__ double solve32(double b, float gs, float &x32) {
+    const MT xv = lin_solve(owns ? (float)b * wsc32 : 0.0f);
+    x32 = owns ? xv * (ssc32 * gs) : 0.0f;
+    return (double)x32;
+  }
+
+  // the triangular solves with the factors in place: v is this thread's
+  // right-hand-side entry, the solution component of its species is returned
+  __device__ __forceinline__ MT lin_solve(MT v) {
     const int nb = (n + DB - 1) / DB;
-    MT v;
-    if constexpr (MIXED) v = owns ? (MT)(b * wsc) : MT(0);
-    else v = owns ? (MT)b : MT(0);
     bsv[tid] = v;
     __syncthreads();
     // forward: L y = P b
@@ -569,25 +618,22 @@ struct CtaCell : Core<CtaCell<MIXED>, false, MIXED> {
     // ys[k] is now the solution component of column k = species k
     const MT xv = owns ? ys[tid] : MT(0);
     __syncthreads();
-    if constexpr (MIXED) return owns ? (double)xv * ssc : 0.0;
-    else return owns ? (double)xv : 0.0;
+    return xv;
   }
 
   // calculate_abundances.c:132-317 for one cell
   __device__ __forceinline__ void run(int cell) {
     const int nspec = A.nspec;
     double *ab = A.abundance + (size_t)cell * nspec;
-    const double n_H = A.density[cell];
     this->rtol = A.reltol;
     this->atol = A.abstol;
     this->mxstep = A.mxstep;
     this->max_total_steps = A.max_total_steps;
     cx = owns ? __ldg(&A.tab.xe_coef[tid]) : 0.0;
-    const double *rate = A.rate + (size_t)cell * A.nreac;
-    for (int r = tid; r < A.nreac; r += blockDim.x)
-      kn[r] = __ldg(&rate[r]) * (__ldg(&A.tab.nh_mask[r]) != 0.0 ? n_H : 1.0);
+    load_rates(A.rate + (size_t)cell * A.nreac, A.density[cell]);
     if (tid == 0) {
       xs[n + 1] = 1.0;
+      xs32[n + 1] = 1.0f;
       part[A.tab.nparts] = 0.0;
       sig[n] = 1.0f;
       sig[n + 1] = 0.0f;
@@ -627,9 +673,9 @@ __global__ void __launch_bounds__(256, 1) chem_cta_kernel(const __grid_constant_
                                                           const int *total_ptr, int mat_smem) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   using MT = typename std::conditional<MIXED, float, double>::type;
-  const CtaLayout L = cta_layout(A.n, A.nreac, A.tab.nparts, A.G, A.ld, sizeof(MT), mat_smem != 0);
+  const CtaLayout L = cta_layout(A.tab, A.ld, sizeof(MT), mat_smem != 0);
   CtaCell<MIXED> c(A, threadIdx.x);
-  c.kn = A.kn_global + (size_t)blockIdx.x * A.nreac;
+  c.kn = A.kn_global + (size_t)blockIdx.x * (A.tab.nkn + 1);
   c.scr = reinterpret_cast<double *>(smem_raw + L.scr);
   c.xs = reinterpret_cast<double *>(smem_raw + L.xs);
   c.part = reinterpret_cast<double *>(smem_raw + L.part);
@@ -637,6 +683,7 @@ __global__ void __launch_bounds__(256, 1) chem_cta_kernel(const __grid_constant_
   c.red_k = reinterpret_cast<unsigned long long *>(smem_raw + L.red + 2 * MAXW * 8);
   c.red_i = reinterpret_cast<int *>(smem_raw + L.red + 2 * MAXW * 16);
   c.sig = reinterpret_cast<float *>(smem_raw + L.sig);
+  c.xs32 = c.sig + (A.n + 2);
   c.perm = reinterpret_cast<int *>(smem_raw + L.perm);
   c.cols = reinterpret_cast<int *>(smem_raw + L.cols);
   c.cnt = c.cols + A.n;
@@ -674,10 +721,10 @@ __global__ void __launch_bounds__(256, 1) eval_cta_kernel(const __grid_constant_
                                                           const double *x, double *out, double *xe_out, int mode,
                                                           int mat_smem) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const CtaLayout L = cta_layout(A.n, A.nreac, A.tab.nparts, A.G, A.ld, 8, mat_smem != 0);
+  const CtaLayout L = cta_layout(A.tab, A.ld, 8, mat_smem != 0);
   CtaCell<false> c(A, threadIdx.x);
   const int n = A.n, tid = threadIdx.x;
-  c.kn = A.kn_global + (size_t)blockIdx.x * A.nreac;
+  c.kn = A.kn_global + (size_t)blockIdx.x * (A.tab.nkn + 1);
   c.scr = reinterpret_cast<double *>(smem_raw + L.scr);
   c.xs = reinterpret_cast<double *>(smem_raw + L.xs);
   c.part = reinterpret_cast<double *>(smem_raw + L.part);
@@ -685,6 +732,7 @@ __global__ void __launch_bounds__(256, 1) eval_cta_kernel(const __grid_constant_
   c.red_k = reinterpret_cast<unsigned long long *>(smem_raw + L.red + 2 * MAXW * 8);
   c.red_i = reinterpret_cast<int *>(smem_raw + L.red + 2 * MAXW * 16);
   c.sig = reinterpret_cast<float *>(smem_raw + L.sig);
+  c.xs32 = c.sig + (A.n + 2);
   c.perm = reinterpret_cast<int *>(smem_raw + L.perm);
   c.cols = reinterpret_cast<int *>(smem_raw + L.cols);
   c.cnt = c.cols + n;
@@ -698,9 +746,7 @@ __global__ void __launch_bounds__(256, 1) eval_cta_kernel(const __grid_constant_
   c.atol = A.abstol;
   c.cx = (tid < n) ? __ldg(&A.tab.xe_coef[tid]) : 0.0;
   for (int s = blockIdx.x; s < nstate; s += gridDim.x) {
-    const double n_H = A.density[s];
-    for (int r = tid; r < A.nreac; r += blockDim.x)
-      c.kn[r] = A.rate[(size_t)s * A.nreac + r] * (__ldg(&A.tab.nh_mask[r]) != 0.0 ? n_H : 1.0);
+    c.load_rates(A.rate + (size_t)s * A.nreac, A.density[s]);
     if (tid == 0) {
       c.xs[n + 1] = 1.0;
       c.part[A.tab.nparts] = 0.0;
@@ -729,13 +775,13 @@ size_t chem_cta_smem(const pdr_net *net, bool mixed, bool *mat_smem) {
   const WarpTables &T = net->cta;
   const int n = T.neq, ld = n | 1;
   const size_t mt = mixed ? 4 : 8;
-  CtaLayout with = cta_layout(n, T.nreac, T.nparts, T.lanes, ld, mt, true);
+  CtaLayout with = cta_layout(T, ld, mt, true);
   int dev = 0, optin = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   if (with.total + 64 <= (size_t)optin) { *mat_smem = true; return with.total; }   // + static shared
   *mat_smem = false;
-  return cta_layout(n, T.nreac, T.nparts, T.lanes, ld, mt, false).total;
+  return cta_layout(T, ld, mt, false).total;
 }
 
 // Per-launch global scratch of the block integrator: rate constants and, when
@@ -745,7 +791,7 @@ size_t chem_cta_global_bytes(const pdr_net *net, bool mixed, int grid) {
   chem_cta_smem(net, mixed, &ms);
   const WarpTables &T = net->cta;
   const int n = T.neq, ld = n | 1;
-  size_t b = al16((size_t)grid * T.nreac * 8);
+  size_t b = al16((size_t)grid * (T.nkn + 1) * 8);
   if (!ms) b += al16((size_t)grid * (n + 2) * ld * (mixed ? 4 : 8));
   return b;
 }
@@ -815,7 +861,7 @@ int launch_chem_cta(const pdr_net *net, int ncell, double *ab, const double *rat
   bool ms = false;
   const size_t smem = chem_cta_smem(net, mixed, &ms);
   A.kn_global = reinterpret_cast<double *>(scratch);
-  A.mat_global = ms ? nullptr : reinterpret_cast<unsigned char *>(scratch) + al16((size_t)grid * T.nreac * 8);
+  A.mat_global = ms ? nullptr : reinterpret_cast<unsigned char *>(scratch) + al16((size_t)grid * (T.nkn + 1) * 8);
   auto k = mixed ? chem_cta_kernel<true> : chem_cta_kernel<false>;
   cudaError_t ea = ensure_smem_attr(mixed, smem);
   if (ea != cudaSuccess) return cuda_fail(ea, "cudaFuncSetAttribute(chem_cta_kernel)");
@@ -852,7 +898,7 @@ int launch_chem_eval_cta(const pdr_net *net, int nstate, const double *x, const 
   cudaError_t e = cudaMalloc(&scratch, chem_cta_global_bytes(net, false, grid));
   if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(eval scratch)");
   A.kn_global = reinterpret_cast<double *>(scratch);
-  A.mat_global = ms ? nullptr : reinterpret_cast<unsigned char *>(scratch) + al16((size_t)grid * T.nreac * 8);
+  A.mat_global = ms ? nullptr : reinterpret_cast<unsigned char *>(scratch) + al16((size_t)grid * (T.nkn + 1) * 8);
   e = cudaFuncSetAttribute(eval_cta_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e == cudaSuccess) {
     eval_cta_kernel<<<grid, T.lanes, smem, st>>>(A, nstate, x, out, xe_out, mode, ms ? 1 : 0);

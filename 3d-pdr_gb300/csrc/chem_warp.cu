@@ -60,6 +60,29 @@ struct ChemArgs {
   int refill_static;        // 1: warp w takes cells w, w+W, ... ; 0: atomic work queue
 };
 
+// byte offsets of one warp's shared arrays (host and device agree)
+struct WarpLayout {
+  size_t kn, scr, xs, part, jrow, sig, ws, total;
+};
+
+__host__ __device__ inline WarpLayout warp_layout(int nsp, const WarpTables &T, bool mixed, bool zsh) {
+  auto al = [](size_t x) { return (x + 15) & ~size_t(15); };
+  WarpLayout L;
+  size_t o = 0;
+  L.kn = o; o += al(8 * (size_t)(T.nkn + 1));   // rate constants, extras, a zero
+  // scr: the RHS operands (FP64) or the two Jacobian scatter buffers (FP32 or FP64 each)
+  size_t scr = (size_t)T.nreac * (mixed ? 8 : 16);
+  if (8 * (size_t)T.nop > scr) scr = 8 * (size_t)T.nop;
+  L.scr = o; o += al(scr);
+  L.xs = o; o += al(8 * (size_t)(nsp + 2));
+  L.part = o; o += al(8 * (size_t)(T.nparts + 1));
+  L.jrow = o; o += al((mixed ? 4 : 8) * (size_t)nsp * (nsp + 3));
+  L.sig = o; o += al(4 * (size_t)(nsp + 2) + 4 * (size_t)nsp + 4 * (size_t)(nsp + 2));   // sig, perm, xs32
+  L.ws = o; o += al(sizeof(CoefShared) + (zsh ? 8 * (QMAX + 1) * kWarp : 0));
+  L.total = o;
+  return L;
+}
+
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
@@ -121,7 +144,22 @@ __device__ __forceinline__ bool lu_rows(MT *a, int ld, int lane, int &mystep, MT
     if (mystep < 0) {
       const MT l = row[k] * rinv;
       row[k] = l;
+#ifdef PDR_LU_SCALAR
       for (int j = k + 1; j < N; j++) row[j] = fma(-l, prow[j], row[j]);
+#else
+      // four columns at a time, every load before any store (the compiler
+      // cannot tell the pivot row and this row apart)
+      int j = k + 1;
+      for (; j + 4 <= N; j += 4) {
+        const MT p0 = prow[j], p1 = prow[j + 1], p2 = prow[j + 2], p3 = prow[j + 3];
+        const MT r0 = row[j], r1 = row[j + 1], r2 = row[j + 2], r3 = row[j + 3];
+        row[j] = fma(-l, p0, r0);
+        row[j + 1] = fma(-l, p1, r1);
+        row[j + 2] = fma(-l, p2, r2);
+        row[j + 3] = fma(-l, p3, r3);
+      }
+      for (; j < N; j++) row[j] = fma(-l, prow[j], row[j]);
+#endif
     }
     __syncwarp();
   }
@@ -163,10 +201,14 @@ struct WarpCell : Core<WarpCell<NSP, MIXED, ZSH>, ZSH, MIXED> {
   MT *jrow;       // [NSP][NSP+3] Newton matrix rows / their LU factors
   float *sig;     // [NSP+2] column scales (mixed)
   int *perm;      // [NSP] pivot lane of each elimination step
+  float *xs32;    // [NSP+2] FP32 copy of the slot values at setup (mixed)
   double cx;      // electron-sum coefficient of species `lane`
+  int cxi;        // the same as an integer
+  bool cx_unit;   // every coefficient of the network is -1, 0 or 1 (warp-uniform)
   int mystep;
   MT invd;
-  double wsc, ssc;   // setup-time weight and its inverse (mixed scaling)
+  double wsc, ssc;      // FP64 form: setup-time weight and its inverse
+  float wsc32, ssc32;   // mixed form: the same in FP32 (the scaling of the FP32 matrix)
 
   __device__ __forceinline__ WarpCell(const ChemArgs &a, int ln) : A(a), lane(ln), owns(ln < NSP) {}
   __device__ __forceinline__ bool leader() const { return lane == 0; }
@@ -175,31 +217,88 @@ struct WarpCell : Core<WarpCell<NSP, MIXED, ZSH>, ZSH, MIXED> {
   __device__ __forceinline__ float sum_all(float v) const { return warp_sum(v); }
   __device__ __forceinline__ double max_all(double v) const { return warp_max(v); }
 
-  // f(y): returns f_lane, records x_e of this call
+  __device__ __forceinline__ void set_xe_coef() {
+    cx = owns ? __ldg(&A.tab.xe_coef[lane]) : 0.0;
+    cxi = (int)cx;
+    cx_unit = __all_sync(FULL, cx == (double)cxi && cxi >= -1 && cxi <= 1);
+  }
+  // this lane's term c_i x_i of x_e: a sign select when the coefficients are
+  // -1, 0 or 1 (every FP64 warp instruction costs an FP64 issue slot)
+  __device__ __forceinline__ double xe_term(double yv) const {
+    if (cx_unit) {
+      const unsigned long long b = (unsigned long long)__double_as_longlong(yv);
+      return (!owns || cxi == 0) ? 0.0 : __longlong_as_double((long long)(cxi < 0 ? (b ^ 0x8000000000000000ull) : b));
+    }
+    return owns ? cx * yv : 0.0;
+  }
+
+  // point the warp's arrays into its shared-memory slice
+  __device__ __forceinline__ void bind(unsigned char *base, const WarpLayout &L) {
+    kn = reinterpret_cast<double *>(base + L.kn);
+    scr = reinterpret_cast<double *>(base + L.scr);
+    xs = reinterpret_cast<double *>(base + L.xs);
+    part = reinterpret_cast<double *>(base + L.part);
+    jrow = reinterpret_cast<MT *>(base + L.jrow);
+    sig = reinterpret_cast<float *>(base + L.sig);
+    perm = reinterpret_cast<int *>(sig + NSP + 2);
+    xs32 = reinterpret_cast<float *>(perm + NSP);
+    this->ws = reinterpret_cast<CoefShared *>(base + L.ws);
+  }
+
+  // per-cell rate constants kn_r = k_r (times n_H for the terms that carry
+  // it), the extras |nu| kn_r of the RHS terms with |nu| > 1, a zero for the
+  // padding terms, and the constants of the slot and partial-sum arrays
+  __device__ __forceinline__ void load_rates(const double *rate, double n_H) {
+    const WarpTables &T = A.tab;
+    for (int r = lane; r < T.nreac; r += kWarp) kn[r] = __ldg(&rate[r]) * (__ldg(&T.nh_mask[r]) != 0.0 ? n_H : 1.0);
+    if (lane == 0) {
+      kn[T.nkn] = 0.0;
+      xs[NSP + 1] = 1.0;
+      part[T.nparts] = 0.0;
+    }
+    __syncwarp();
+    for (int e = lane; e < T.nkext; e += kWarp) {
+      const int2 q = __ldg(&T.kext[e]);
+      kn[T.nreac + e] = (double)q.y * kn[q.x];
+    }
+    __syncwarp();
+  }
+
+  // f(y): returns f_lane, records x_e of this call.  The operands are this
+  // state's slot values and the products x_a x_b of the two-body reactant
+  // pairs (one FP64 multiply per pair instead of two per reaction); every
+  // stoichiometric term is then one FMA with the signed rate constant.
   __device__ __forceinline__ double rhs(double yv) {
     const WarpTables &T = A.tab;
-    if (owns) xs[lane] = yv;
-    const double xe = warp_sum(owns ? cx * yv : 0.0);
-    if (lane == 0) xs[NSP] = xe;
+    double *P = scr;
+    if (owns) P[lane] = yv;
+    const double xe = warp_sum(xe_term(yv));
+    if (lane == 0) {
+      P[NSP] = xe;
+      P[NSP + 1] = 1.0;
+    }
     this->xe_last = xe;
     __syncwarp();
-    for (int r = lane; r < T.nreac; r += kWarp) {
-      const int2 ab = __ldg(&T.rab[r]);
-      scr[r] = kn[r] * xs[ab.x] * xs[ab.y];
+    for (int p = lane; p < T.npairs; p += kWarp) {
+      const int2 ab = __ldg(&T.pairs[p]);
+      P[NSP + 2 + p] = P[ab.x] * P[ab.y];
     }
     __syncwarp();
     double s = 0.0;
 #pragma unroll 2
     for (int t = 0; t < T.rhs_len; t++) {
-      const int rf = __ldg(&T.rhs_rf[t * kWarp + lane]);
-      const double nu = __ldg(&T.rhs_nu[t * kWarp + lane]);
-      s = fma(nu, scr[rf & 0xffff], s);
-      const int fl = (rf >> 16) - 1;
+      const int2 d = __ldg(&T.rhs_t[t * kWarp + lane]);
+      const double k = kn[d.x & 0xffff];
+      // nu kn_r with nu = +-1 (|nu| > 1 reads its extra constant): the sign
+      // bit of kn_r flipped in the integer pipe
+      const double ks = __hiloint2double(__double2hiint(k) ^ (d.y & (int)0x80000000u), __double2loint(k));
+      s = fma(ks, P[d.y & 0x7fffffff], s);
+      const int fl = (int)((unsigned)d.x >> 16) - 1;
       if (fl >= 0) { part[fl] = s; s = 0.0; }
     }
     __syncwarp();
-    double f = 0.0;
-    for (int k = 0; k < T.plist_len; k++) f += part[__ldg(&T.plist[k * kWarp + lane])];
+    double f = part[__ldg(&T.plist[lane])];
+    for (int k = 1; k < T.plist_len; k++) f += part[__ldg(&T.plist[k * kWarp + lane])];
     __syncwarp();
     this->nfe++;
     return owns ? f : 0.0;
@@ -210,25 +309,38 @@ struct WarpCell : Core<WarpCell<NSP, MIXED, ZSH>, ZSH, MIXED> {
   __device__ __forceinline__ void assemble(double yv, double rf_d, bool identity) {
     const WarpTables &T = A.tab;
     if (owns) xs[lane] = yv;
-    const double xe = warp_sum(owns ? cx * yv : 0.0);
+    const double xe = warp_sum(xe_term(yv));
     if (lane == 0) xs[NSP] = xe;
     if constexpr (MIXED) {
-      // column scales 1/w_j = rtol|y_j|+atol, normalised by atol so they fit FP32
-      ssc = this->rtol * fabs(yv) + this->atol;
-      wsc = 1.0 / ssc;
-      if (owns) sig[lane] = (float)(ssc / this->atol);
-      if (lane == 0) { sig[NSP] = 1.0f; sig[NSP + 1] = 0.0f; }
+      // column scales 1/w_j = rtol|y_j|+atol, normalised by atol so they fit
+      // FP32, formed in FP32 (the matrix is FP32; y and x_e converted once)
+      const float y32 = (float)yv;
+      ssc32 = fmaf(this->rtol32, fabsf(y32), this->atol32);
+      wsc32 = __frcp_rn(ssc32);
+      if (owns) {
+        sig[lane] = ssc32 * __frcp_rn(this->atol32);
+        xs32[lane] = y32;
+      }
+      if (lane == 0) {
+        sig[NSP] = 1.0f;
+        sig[NSP + 1] = 0.0f;
+        xs32[NSP] = (float)xe;
+        xs32[NSP + 1] = 1.0f;
+      }
     }
     __syncwarp();
     MT *Da = reinterpret_cast<MT *>(scr);
     MT *Db = Da + T.nreac;
     for (int r = lane; r < T.nreac; r += kWarp) {
       const int2 ab = __ldg(&T.rab[r]);
-      const double k = kn[r];
       if constexpr (MIXED) {
-        Da[r] = (float)(k * xs[ab.y]) * sig[ab.x];
-        Db[r] = (float)(k * xs[ab.x]) * sig[ab.y];
+        // dphi_r/dx_a and dphi_r/dx_b, column-scaled, in FP32: one conversion
+        // of the rate constant per reaction
+        const float k32 = (float)kn[r];
+        Da[r] = k32 * (xs32[ab.y] * sig[ab.x]);
+        Db[r] = k32 * (xs32[ab.x] * sig[ab.y]);
       } else {
+        const double k = kn[r];
         Da[r] = k * xs[ab.y];
         Db[r] = (ab.y == NSP + 1) ? 0.0 : k * xs[ab.x];
       }
@@ -237,6 +349,7 @@ struct WarpCell : Core<WarpCell<NSP, MIXED, ZSH>, ZSH, MIXED> {
     if (owns)
       for (int j = 0; j < NSP + 2; j++) row[j] = MT(0);
     __syncwarp();
+#ifdef PDR_JAC_ROWS
     if (owns) {
       for (int t = 0; t < T.jac_len; t++) {
         MT nu;
@@ -250,9 +363,48 @@ struct WarpCell : Core<WarpCell<NSP, MIXED, ZSH>, ZSH, MIXED> {
       }
     }
     __syncwarp();
+#else
+    // term-parallel: the (row, column) contributions nu * dphi_r/dx_col sorted
+    // by entry and cut into 32 balanced chunks; a lane sums each run of one
+    // entry in a register and stores it, and a run that crosses a chunk
+    // boundary leaves partials in slots (the RHS partial-sum buffer, free
+    // here) that a second pass adds in chunk order.  The rows of the electron
+    // and hydrogen hold most contributions: walking one row per lane left the
+    // warp waiting on those two lanes.
+    {
+      MT *slots = reinterpret_cast<MT *>(part);
+      MT s = MT(0);
+#pragma unroll 2
+      for (int t = 0; t < T.hlen; t++) {
+        const int x = __ldg(&T.h_x[t * kWarp + lane]);
+        const int y = __ldg(&T.h_y[t * kWarp + lane]);
+        MT nu;
+        if constexpr (MIXED) nu = __ldg(&T.h_nu_f[t * kWarp + lane]);
+        else nu = __ldg(&T.h_nu[t * kWarp + lane]);
+        const int r = x & 0xffff;
+        s = fma(nu, (x & 0x10000) ? Db[r] : Da[r], s);
+        const int kind = (x >> 17) & 3;
+        if (kind == 1) {
+          jrow[(y & 0xff) * (NSP + 3) + ((y >> 8) & 0xff)] = s;
+          s = MT(0);
+        } else if (kind == 2) {
+          slots[y >> 16] = s;
+          s = MT(0);
+        }
+      }
+      __syncwarp();
+      for (int b = lane; b < T.nbnd; b += kWarp) {
+        const int tt = __ldg(&T.bnd_t[b]), ss = __ldg(&T.bnd_s[b]);
+        MT acc = MT(0);
+        for (int q = ss & 0xffff; q < (ss >> 16); q++) acc += slots[q];
+        jrow[(tt & 0xff) * (NSP + 3) + ((tt >> 8) & 0xff)] = acc;
+      }
+      __syncwarp();
+    }
+#endif
     const MT e = owns ? row[NSP] : MT(0);
     MT rf;
-    if constexpr (MIXED) rf = (MT)(rf_d * (wsc * this->atol));   // row weight, normalised like the columns
+    if constexpr (MIXED) rf = (MT)rf_d * (wsc32 * this->atol32);   // row weight, normalised like the columns
     else rf = (MT)rf_d;
 #pragma unroll 4
     for (int j = 0; j < NSP; j++) {
@@ -280,33 +432,29 @@ struct WarpCell : Core<WarpCell<NSP, MIXED, ZSH>, ZSH, MIXED> {
   }
 
   __device__ __forceinline__ double solve(double b) {
-    double x;
-    if constexpr (MIXED) {
-      const float xs_ = lu_solve_rows<NSP, float>(jrow, NSP + 3, lane, mystep, invd, (float)(b * wsc), perm);
-      x = (double)xs_ * ssc;
-    } else {
-      x = lu_solve_rows<NSP, double>(jrow, NSP + 3, lane, mystep, invd, b, perm);
-    }
+    const double x = lu_solve_rows<NSP, double>(jrow, NSP + 3, lane, mystep, invd, b, perm);
     return owns ? x : 0.0;
+  }
+
+  // mixed form: the residual is converted once and scaled in FP32 (the
+  // scaling of the FP32 matrix), the correction comes back times ssc*gscale,
+  // in FP32 for the norm and in FP64 for the state
+  __device__ __forceinline__ double solve32(double b, float gs, float &x32) {
+    const float xv = lu_solve_rows<NSP, float>(jrow, NSP + 3, lane, mystep, invd, (float)b * wsc32, perm);
+    x32 = owns ? xv * (ssc32 * gs) : 0.0f;
+    return (double)x32;
   }
 
   // calculate_abundances.c:132-317 for one cell
   __device__ __forceinline__ void run(int cell) {
     const int nspec = A.nspec;
     double *ab = A.abundance + (size_t)cell * nspec;
-    const double n_H = A.density[cell];
     this->rtol = A.reltol;
     this->atol = A.abstol;
     this->mxstep = A.mxstep;
     this->max_total_steps = A.max_total_steps;
-    cx = owns ? __ldg(&A.tab.xe_coef[lane]) : 0.0;
-    // per-cell rate constants, multiplied by n_H for two-body terms
-    const double *rate = A.rate + (size_t)cell * A.nreac;
-    for (int r = lane; r < A.nreac; r += kWarp) kn[r] = __ldg(&rate[r]) * (__ldg(&A.tab.nh_mask[r]) != 0.0 ? n_H : 1.0);
-    if (lane == 0) {
-      xs[NSP + 1] = 1.0;
-      part[A.tab.nparts] = 0.0;
-    }
+    set_xe_coef();
+    load_rates(A.rate + (size_t)cell * A.nreac, A.density[cell]);
 #pragma unroll
     for (int j = 0; j <= QMAX; j++) this->z[j] = 0.0;
     this->z[0] = owns ? ab[lane] : 0.0;
@@ -353,26 +501,10 @@ __global__ void __launch_bounds__(RegVariant<RV>::threads, RegVariant<RV>::min_b
   extern __shared__ __align__(16) unsigned char smem_raw[];
   using MT = typename std::conditional<MIXED, float, double>::type;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int nreac = A.nreac;
-  // per-warp shared layout
-  // scr: the fluxes (FP64) or the two Jacobian scatter buffers (MT each)
-  const size_t kn_b = (size_t)nreac * 8, scr_b = (size_t)nreac * (MIXED ? 8 : 16), xs_b = 8 * (NSP + 2);
-  const size_t part_b = 8 * (A.tab.nparts + 1);
   constexpr bool ZSH = RegVariant<RV>::zsh;
-  const size_t jrow_b = sizeof(MT) * NSP * (NSP + 3), sig_b = 4 * (NSP + 2) + 4 * NSP;
-  const size_t ws_b = sizeof(CoefShared) + (ZSH ? 8 * (QMAX + 1) * kWarp : 0);
-  auto al = [](size_t x) { return (x + 15) & ~size_t(15); };
-  const size_t per_warp = al(kn_b) + al(scr_b) + al(xs_b) + al(part_b) + al(jrow_b) + al(sig_b) + al(ws_b);
-  unsigned char *base = smem_raw + per_warp * warp;
+  const WarpLayout L = warp_layout(NSP, A.tab, MIXED, ZSH);
   WarpCell<NSP, MIXED, ZSH> c(A, lane);
-  c.kn = reinterpret_cast<double *>(base);
-  c.scr = reinterpret_cast<double *>(base + al(kn_b));
-  c.xs = reinterpret_cast<double *>(base + al(kn_b) + al(scr_b));
-  c.part = reinterpret_cast<double *>(base + al(kn_b) + al(scr_b) + al(xs_b));
-  c.jrow = reinterpret_cast<MT *>(base + al(kn_b) + al(scr_b) + al(xs_b) + al(part_b));
-  c.sig = reinterpret_cast<float *>(base + al(kn_b) + al(scr_b) + al(xs_b) + al(part_b) + al(jrow_b));
-  c.perm = reinterpret_cast<int *>(c.sig + NSP + 2);
-  c.ws = reinterpret_cast<CoefShared *>(base + al(kn_b) + al(scr_b) + al(xs_b) + al(part_b) + al(jrow_b) + al(sig_b));
+  c.bind(smem_raw + L.total * warp, L);
   if constexpr (ZSH) {
     c.z.p = reinterpret_cast<double *>(reinterpret_cast<unsigned char *>(c.ws) + sizeof(CoefShared)) + lane;
     c.z.s = kWarp;
@@ -402,31 +534,16 @@ __global__ void __launch_bounds__(128) eval_kernel(const __grid_constant__ ChemA
                                                    const double *x, double *out, double *xe_out, int mode) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int nreac = A.nreac;
-  auto al = [](size_t v) { return (v + 15) & ~size_t(15); };
-  const size_t kn_b = (size_t)nreac * 8, scr_b = (size_t)nreac * 16, xs_b = 8 * (NSP + 2);
-  const size_t part_b = 8 * (A.tab.nparts + 1), jrow_b = 8 * NSP * (NSP + 3), sig_b = 4 * (NSP + 2) + 4 * NSP;
-  const size_t per_warp = al(kn_b) + al(scr_b) + al(xs_b) + al(part_b) + al(jrow_b) + al(sig_b) + al(sizeof(CoefShared));
-  unsigned char *base = smem_raw + per_warp * warp;
+  const WarpLayout L = warp_layout(NSP, A.tab, false, false);
   WarpCell<NSP, false, false> c(A, lane);
-  c.kn = reinterpret_cast<double *>(base);
-  c.scr = reinterpret_cast<double *>(base + al(kn_b));
-  c.xs = reinterpret_cast<double *>(base + al(kn_b) + al(scr_b));
-  c.part = reinterpret_cast<double *>(base + al(kn_b) + al(scr_b) + al(xs_b));
-  c.jrow = reinterpret_cast<double *>(base + al(kn_b) + al(scr_b) + al(xs_b) + al(part_b));
-  c.sig = reinterpret_cast<float *>(base + al(kn_b) + al(scr_b) + al(xs_b) + al(part_b) + al(jrow_b));
-  c.perm = reinterpret_cast<int *>(c.sig + NSP + 2);
-  c.ws = reinterpret_cast<CoefShared *>(base + al(kn_b) + al(scr_b) + al(xs_b) + al(part_b) + al(jrow_b) + al(sig_b));
+  c.bind(smem_raw + L.total * warp, L);
   c.rtol = A.reltol;
   c.mxstep = A.mxstep;
   c.max_total_steps = A.max_total_steps;
   c.atol = A.abstol;
-  c.cx = (lane < NSP) ? __ldg(&A.tab.xe_coef[lane]) : 0.0;
+  c.set_xe_coef();
   for (int s = blockIdx.x * (blockDim.x >> 5) + warp; s < nstate; s += gridDim.x * (blockDim.x >> 5)) {
-    const double n_H = A.density[s];
-    for (int r = lane; r < nreac; r += kWarp) c.kn[r] = A.rate[(size_t)s * nreac + r] * (A.tab.nh_mask[r] != 0.0 ? n_H : 1.0);
-    if (lane == 0) { c.xs[NSP + 1] = 1.0; c.part[A.tab.nparts] = 0.0; }
-    __syncwarp();
+    c.load_rates(A.rate + (size_t)s * A.nreac, A.density[s]);
     const double yv = (lane < NSP) ? x[(size_t)s * NSP + lane] : 0.0;
     if (mode == 0) {
       const double f = c.rhs(yv);
@@ -444,12 +561,8 @@ __global__ void __launch_bounds__(128) eval_kernel(const __grid_constant__ ChemA
 
 }  // namespace
 
-size_t chem_warp_smem_per_warp(int nsp, int nreac, int nparts, bool mixed, bool zshared) {
-  auto al = [](size_t x) { return (x + 15) & ~size_t(15); };
-  const size_t mt = mixed ? 4 : 8;
-  return al((size_t)nreac * 8) + al((size_t)nreac * (mixed ? 8 : 16)) + al(8 * (nsp + 2)) + al(8 * (nparts + 1)) +
-         al(mt * nsp * (nsp + 3)) + al(4 * (nsp + 2) + 4 * nsp) +
-         al(sizeof(CoefShared) + (zshared ? 8 * (QMAX + 1) * kWarp : 0));
+size_t chem_warp_smem_per_warp(const WarpTables &T, bool mixed, bool zshared) {
+  return warp_layout(T.neq, T, mixed, zshared).total;
 }
 
 // Launch the persistent warp kernel over `ncell` cells (or the cells listed in
@@ -492,7 +605,7 @@ int launch_chem_warp(const pdr_net *net, int ncell, double *ab, const double *ra
   if (wpb > 8) return PDR_E_ARG;
   if (rv >= 2 && wpb > 4) return PDR_E_ARG;   // those variants launch at most 128 threads per block
   const bool zsh = (rv == 1 || rv == 3);
-  const size_t smem = chem_warp_smem_per_warp(32, A.nreac, T.nparts, mixed, zsh) * wpb;
+  const size_t smem = chem_warp_smem_per_warp(T, mixed, zsh) * wpb;
   const int variant = (mixed ? 4 : 0) + rv;
   using KFn = void (*)(ChemArgs, int, const int *);
   static const KFn kernels[8] = {chem_warp_kernel<32, false, 0>, chem_warp_kernel<32, false, 1>,
@@ -552,7 +665,7 @@ int launch_chem_eval(const pdr_net *net, int nstate, const double *x, const doub
   A.density = dens;
   A.reltol = 1e-8;
   A.abstol = 1e-30;
-  const size_t smem = chem_warp_smem_per_warp(32, A.nreac, T.nparts, false, false) * 4;
+  const size_t smem = chem_warp_smem_per_warp(T, false, false) * 4;
   auto k = eval_kernel<32>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(eval)");

@@ -8,6 +8,7 @@
 // tables the kernels read: reactant slots per reaction, the net stoichiometry as
 // per-species term lists, and their balanced split over the 32 lanes of a warp.
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <fstream>
@@ -242,11 +243,48 @@ int build_device_tables(pdr_net *net) {
     w.nreac = h.nreac;
     w.lanes = G;
     const int T = (int)terms.size();
-    // RHS: the sorted term list cut into G balanced chunks; a chunk flushes
-    // its running sum into a partial slot whenever the species changes
+    // RHS operands: the slot values themselves (one-body reactions, whose
+    // flux is kn x_a) and the product x_a x_b of every distinct reactant pair
+    // of the two-body reactions, formed once per RHS evaluation.  A term is
+    // then one FMA, s += (nu kn_r) * operand, with nu kn_r taken from the
+    // per-cell rate constants: nu = +-1 is a sign flip of kn_r (an integer
+    // operation), |nu| > 1 reads an extra constant |nu| kn_r made once per cell.
+    std::vector<int> op_of(h.nreac, ONE);
+    std::map<std::pair<int, int>, int> pair_index;
+    std::vector<int2> pairs;
+    for (int r = 0; r < h.nreac; r++) {
+      if (h.ode_kind[r] == ODE_XRAY) continue;
+      const int2 ab = rab[r];
+      if (h.ode_kind[r] == ODE_BI) {
+        const std::pair<int, int> key(std::min(ab.x, ab.y), std::max(ab.x, ab.y));
+        auto it = pair_index.find(key);
+        if (it == pair_index.end()) {
+          it = pair_index.emplace(key, (int)pairs.size()).first;
+          pairs.push_back(make_int2(key.first, key.second));
+        }
+        op_of[r] = neq + 2 + it->second;
+      } else {
+        op_of[r] = ab.x;
+      }
+    }
+    std::map<std::pair<int, int>, int> ext_index;
+    std::vector<int2> kext;   // (reaction, |nu|) of the extra constants
+    auto kidx_of = [&](int r, double nu) {
+      const int m = (int)std::fabs(nu);
+      if (m == 1) return r;
+      auto it = ext_index.find({r, m});
+      if (it == ext_index.end()) {
+        it = ext_index.emplace(std::make_pair(r, m), (int)kext.size()).first;
+        kext.push_back(make_int2(r, m));
+      }
+      return h.nreac + it->second;
+    };
+    for (auto &t : terms)
+      if (std::fabs(t.nu) != std::floor(std::fabs(t.nu)) || std::fabs(t.nu) > 64) return PDR_E_NET;
+    // the sorted term list cut into G balanced chunks; a chunk flushes its
+    // running sum into a partial slot whenever the species changes
     w.rhs_len = std::max(1, (T + G - 1) / G);
-    std::vector<int> rf(w.rhs_len * G, 0);
-    std::vector<double> nu(w.rhs_len * G, 0.0);
+    std::vector<int2> rt(w.rhs_len * G, make_int2(0, ONE));   // padding: 0 * x_one
     std::vector<std::vector<int>> parts(G);
     int slot = 0;
     for (int l = 0; l < G; l++) {
@@ -258,11 +296,22 @@ int build_device_tables(pdr_net *net) {
           parts[terms[t].i].push_back(slot);
           slot++;
         }
-        rf[k * G + l] = terms[t].r | ((fl + 1) << 16);
-        nu[k * G + l] = terms[t].nu;
+        const int kidx = kidx_of(terms[t].r, terms[t].nu);
+        rt[k * G + l] = make_int2(kidx | ((fl + 1) << 16),
+                                  op_of[terms[t].r] | (terms[t].nu < 0 ? (int)0x80000000u : 0));
       }
     }
-    if (slot + 1 >= 65536) return PDR_E_NET;
+    // padding terms read the constant-zero rate slot nkn (kn is zero-filled there)
+    const int nkn = h.nreac + (int)kext.size();
+    for (int l = 0; l < G; l++) {
+      int b = l * w.rhs_len, e = std::min(T, b + w.rhs_len);
+      for (int t = std::max(e, b); t < b + w.rhs_len; t++) rt[(t - b) * G + l] = make_int2(nkn, ONE);
+    }
+    if (slot + 1 >= 65536 || nkn + 1 >= 65536) return PDR_E_NET;
+    w.nkn = nkn;
+    w.nkext = (int)kext.size();
+    w.npairs = (int)pairs.size();
+    w.nop = neq + 2 + w.npairs;
     w.nparts = slot;
     w.plist_len = 1;
     for (auto &p : parts) w.plist_len = std::max<int>(w.plist_len, (int)p.size());
@@ -286,12 +335,11 @@ int build_device_tables(pdr_net *net) {
       }
     std::vector<double> xe(G, 0.0);
     for (int i = 0; i < neq; i++) xe[i] = h.xe[i];
-    // term-parallel Jacobian tables (block integrator only: in the warp
-    // integrator the per-row lists measured as fast)
+    // term-parallel Jacobian tables (both integrators)
     std::vector<int> hx, hy, bt, bs;
     std::vector<double> hn;
     std::vector<float> hnf;
-    if (G > kWarp) {
+    {
       struct Half { int i, col, r, which; double nu; };
       std::vector<Half> hs;
       for (auto &t : terms) {
@@ -339,21 +387,26 @@ int build_device_tables(pdr_net *net) {
         }
         e0 = e1;
       }
-      // the slots live in the block integrator's LU panel buffer (8 x neq values)
-      if (slot > 8 * neq || neq + 1 > 255) return PDR_E_NET;
+      // the slots live in the block integrator's LU panel buffer (8 x neq
+      // values) and in the warp integrator's RHS partial-sum buffer (nparts
+      // values, free during the assembly); a run crosses at most G-1 chunk
+      // boundaries in all
+      if (neq + 1 > 255) return PDR_E_NET;
+      if (G > kWarp ? slot > 8 * neq : slot > w.nparts) return PDR_E_NET;
       w.nbnd = (int)bt.size();
     }
     int rc2 = 0;
     w.rab = upload(net, rab, rc2);
     w.nh_mask = upload(net, nhm, rc2);
-    w.rhs_rf = upload(net, rf, rc2);
-    w.rhs_nu = upload(net, nu, rc2);
+    w.rhs_t = upload(net, rt, rc2);
+    w.pairs = upload(net, pairs, rc2);
+    w.kext = upload(net, kext, rc2);
     w.plist = upload(net, pl, rc2);
     w.jac_rab = upload(net, jr, rc2);
     w.jac_nu = upload(net, jn, rc2);
     w.jac_nu_f = upload(net, jnf, rc2);
     w.xe_coef = upload(net, xe, rc2);
-    if (G > kWarp) {
+    {
       w.h_x = upload(net, hx, rc2);
       w.h_y = upload(net, hy, rc2);
       w.h_nu = upload(net, hn, rc2);

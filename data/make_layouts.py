@@ -74,4 +74,7 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PDR_REFERENCE")
+    if not ref:
+        raise SystemExit("usage: python data/make_layouts.py <3D-PDR source tree> (or set PDR_REFERENCE)")
+    main(ref)

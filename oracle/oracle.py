@@ -49,8 +49,8 @@ def _ptr(a, t=_dp):
     return a.ctypes.data_as(t)
 
 
-def _load():
-    path = os.path.join(HERE, "liboracle.so")
+def _load(opt="O2"):
+    path = os.path.join(HERE, "liboracle.so" if opt == "O2" else f"liboracle_{opt}.so")
     if not os.path.exists(path):
         raise RuntimeError("oracle not built: run `make -C oracle` (or __graft_entry__.build())")
     lib = C.CDLL(path)
@@ -112,14 +112,15 @@ def _load():
     return lib
 
 
-_LIB = None
+_LIBS = {}
 
 
-def lib():
-    global _LIB
-    if _LIB is None:
-        _LIB = _load()
-    return _LIB
+def lib(opt="O2"):
+    """The oracle library: "O2" (default) or "O0" (the same sources built at the
+    reference's own C optimisation level, for the CPU baseline)."""
+    if opt not in _LIBS:
+        _LIBS[opt] = _load(opt)
+    return _LIBS[opt]
 
 
 NETWORKS = {"reduced": 0, "full": 1, "mynetwork": 2}
@@ -135,17 +136,18 @@ class Network:
     generated code (data/layout_<name>.d); "file": species-file order with
     charges from the species names."""
 
-    def __init__(self, name, data_dir=DATA, layout="reference"):
+    def __init__(self, name, data_dir=DATA, layout="reference", opt="O2"):
         self.name = name
+        self.L = lib(opt)
         err = C.create_string_buffer(256)
         sp = os.path.join(data_dir, f"species_{name}.d").encode()
         rp = os.path.join(data_dir, f"rates_{name}.d").encode()
-        self.p = lib().orc_net_load(sp, rp, err, 256)
+        self.p = self.L.orc_net_load(sp, rp, err, 256)
         if not self.p:
             raise RuntimeError(err.value.decode())
         lay = os.path.join(data_dir, f"layout_{name}.d")
         if layout == "reference" and os.path.exists(lay):
-            if lib().orc_net_load_layout(self.p, lay.encode(), err, 256):
+            if self.L.orc_net_load_layout(self.p, lay.encode(), err, 256):
                 raise RuntimeError(err.value.decode())
         n = self.p.contents
         self.nspec, self.nreac, self.neq = n.nspec, n.nreac, n.neq
@@ -159,7 +161,7 @@ class Network:
 
     def __del__(self):
         try:
-            lib().orc_net_free(self.p)
+            self.L.orc_net_free(self.p)
         except Exception:
             pass
 
@@ -168,21 +170,21 @@ class Network:
         x = np.ascontiguousarray(x, dtype=np.float64)
         ode = np.zeros(self.neq)
         xe = C.c_double()
-        lib().orc_rhs(self.p, _ptr(rate), n_H, _ptr(x), _ptr(ode), C.byref(xe))
+        self.L.orc_rhs(self.p, _ptr(rate), n_H, _ptr(x), _ptr(ode), C.byref(xe))
         return ode, xe.value
 
     def jac(self, rate, n_H, x):
         rate = np.ascontiguousarray(rate, dtype=np.float64)
         x = np.ascontiguousarray(x, dtype=np.float64)
         J = np.zeros((self.neq, self.neq))
-        lib().orc_jac(self.p, _ptr(rate), n_H, _ptr(x), _ptr(J))
+        self.L.orc_jac(self.p, _ptr(rate), n_H, _ptr(x), _ptr(J))
         return J
 
     def jac_xe_const(self, rate, n_H, x, x_e):
         rate = np.ascontiguousarray(rate, dtype=np.float64)
         x = np.ascontiguousarray(x, dtype=np.float64)
         J = np.zeros((self.neq, self.neq))
-        lib().orc_jac_xe_const(self.p, _ptr(rate), n_H, _ptr(x), x_e, _ptr(J))
+        self.L.orc_jac_xe_const(self.p, _ptr(rate), n_H, _ptr(x), x_e, _ptr(J))
         return J
 
     def calculate_abundances(self, abundance, rate, density, temperature, reltol=1e-8,
@@ -195,9 +197,9 @@ class Network:
         temp = np.ascontiguousarray(temperature, dtype=np.float64)
         npart = ab.shape[0]
         stats = np.zeros((npart, 8), dtype=np.int64) if want_stats else None
-        st = lib().orc_calculate_abundances(self.p, _ptr(ab), _ptr(rate), _ptr(dens), _ptr(temp),
-                                            npart, reltol, abstol, start_time, end_time, nthreads,
-                                            _ptr(stats, _lp) if want_stats else None)
+        st = self.L.orc_calculate_abundances(self.p, _ptr(ab), _ptr(rate), _ptr(dens), _ptr(temp),
+                                             npart, reltol, abstol, start_time, end_time, nthreads,
+                                             _ptr(stats, _lp) if want_stats else None)
         return (ab, st, stats) if want_stats else (ab, st)
 
     def rates(self, phys, T, Td, rad_surface, AV, column5, nthreads=0, zeta=None):
@@ -218,16 +220,16 @@ class Network:
         nrays = rad_surface.shape[1]
         out = np.zeros((ncell, self.nreac))
         args = [np.ascontiguousarray(a, dtype=np.float64) for a in (Td, rad_surface, AV, column5)]
-        st = lib().orc_rates_batched(self.p, C.byref(phys), ncell, nrays, _ptr(T),
-                                     *[_ptr(a) for a in args], _ptr(out), nthreads)
+        st = self.L.orc_rates_batched(self.p, C.byref(phys), ncell, nrays, _ptr(T),
+                                      *[_ptr(a) for a in args], _ptr(out), nthreads)
         return out, st
 
     def rates_cell(self, phys, T, Td, rad_surface, AV, column5):
         out = np.zeros(self.nreac)
         nr = np.zeros(6, dtype=np.int32)
         args = [np.ascontiguousarray(a, dtype=np.float64) for a in (rad_surface, AV, column5)]
-        st = lib().orc_rates_cell(self.p, C.byref(phys), T, Td, len(rad_surface),
-                                  *[_ptr(a) for a in args], _ptr(out), _ptr(nr, _ip))
+        st = self.L.orc_rates_cell(self.p, C.byref(phys), T, Td, len(rad_surface),
+                                   *[_ptr(a) for a in args], _ptr(out), _ptr(nr, _ip))
         return out, nr, st
 
 

@@ -22,7 +22,9 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 import oracle as O  # noqa: E402
 
-REF = os.environ.get("PDR_REFERENCE", "/root/reference")
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PDR_REFERENCE", "")
+if not os.path.exists(os.path.join(REF, "modules.F90")):
+    raise SystemExit("usage: python tests/golden/make_golden.py <3D-PDR source tree> (or set PDR_REFERENCE)")
 
 
 def fortran_numbers(text):

@@ -14,7 +14,9 @@ import pytest
 import fin as F
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-BENCH = os.path.join(os.environ.get("PDR_REFERENCE_DIR", "/root/reference"), "Benchmarks.tgz")
+import build  # noqa: E402  (the build recipe knows where the reference tree is, if anywhere)
+
+BENCH = os.path.join(build.reference_dir() or "", "Benchmarks.tgz")
 NLEV = {"CII": 5, "CI": 5, "OI": 5, "CO": 41}
 
 
