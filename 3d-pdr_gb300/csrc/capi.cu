@@ -31,11 +31,11 @@ size_t chem_warp_smem_per_warp(const WarpTables &T, bool mixed, bool zshared);
 int launch_chem_warp(const pdr_net *net, int ncell, double *ab, const double *rate, const double *dens,
                      const double *tend, const pdr_chem_opts &o, int *status, int *stats, int *queue,
                      int *fb_list, int *fb_count, const int *cell_list, const int *total_ptr, bool mixed,
-                     int sm_count, cudaStream_t st);
+                     int sm_count, cudaStream_t st, const int *sm_limit = nullptr);
 int launch_chem_cta(const pdr_net *net, int ncell, double *ab, const double *rate, const double *dens,
                     const double *tend, const pdr_chem_opts &o, int *status, int *stats, int *queue,
                     int *fb_list, int *fb_count, const int *cell_list, const int *total_ptr, bool mixed,
-                    int grid, void *scratch, cudaStream_t st);
+                    int grid, void *scratch, cudaStream_t st, const int *sm_limit = nullptr, int grid_sms = 1);
 size_t chem_cta_global_bytes(const pdr_net *net, bool mixed, int grid);
 size_t chem_cta_smem(const pdr_net *net, bool mixed, bool *mat_smem);
 int chem_cta_blocks_per_sm(const pdr_net *net, bool mixed);
@@ -100,6 +100,7 @@ struct Scratch {
   size_t redo_cap = 0;
   void *cta = nullptr;       // block integrator: per-block rate constants (and matrices)
   size_t cta_bytes = 0;
+  int *sm_limit = nullptr;   // solver instances: SMs their running launch may keep (null: all)
 };
 static std::mutex g_mu;
 static Scratch g_scratch[64];
@@ -205,11 +206,11 @@ static int solve_core(const pdr_net *net, int ncell, double *ab, const double *r
   if (uses_warp_path(net, o)) {
     const int sm_use = eff_sms(o, sms);
     rc = launch_chem_warp(net, ncell, ab, rate, dens, tend, o, status, stats, s->counters + 0, s->redo,
-                          s->counters + 2, nullptr, nullptr, mixed, sm_use, st);
+                          s->counters + 2, nullptr, nullptr, mixed, sm_use, st, s->sm_limit);
     if (rc || !mixed) return rc;
     // cells whose FP32 Newton iteration failed are re-solved in FP64
     return launch_chem_warp(net, ncell, ab, rate, dens, tend, o, status, stats, s->counters + 1, nullptr, nullptr,
-                            s->redo, s->counters + 2, false, sm_use, st);
+                            s->redo, s->counters + 2, false, sm_use, st, s->sm_limit);
   }
   // one block per cell: persistent grid of SMs x resident blocks, or (refill
   // 2) one block per cell and no persistence, which needs the Newton matrix in
@@ -233,10 +234,11 @@ static int solve_core(const pdr_net *net, int ncell, double *ab, const double *r
     return PDR_E_ARG;
   }
   rc = launch_chem_cta(net, ncell, ab, rate, dens, tend, o, status, stats, s->counters + 0, s->redo, s->counters + 2,
-                       nullptr, nullptr, mixed, grid_main, s->cta, st);
+                       nullptr, nullptr, mixed, grid_main, s->cta, st, s->sm_limit, eff_sms(o, sms));
   if (rc || !mixed) return rc;
   return launch_chem_cta(net, ncell, ab, rate, dens, tend, o, status, stats, s->counters + 1, nullptr, nullptr,
-                         s->redo, s->counters + 2, false, cta_grid(net, o, false, sms), s->cta, st);
+                         s->redo, s->counters + 2, false, cta_grid(net, o, false, sms), s->cta, st, s->sm_limit,
+                         eff_sms(o, sms));
 }
 
 }  // namespace pdr
@@ -248,6 +250,7 @@ struct pdr_solver {
   pdr_chem_opts opts;
   int max_cells = 0, sms = 0, dev = 0;
   pdr::Scratch s;
+  int *h_words = nullptr;   // pinned: [0] "no limit" (a large SM count), [1] the latest limit
 };
 
 namespace pdr {
@@ -376,6 +379,15 @@ int pdr_solver_create(const pdr_net *net, int max_cells, const pdr_chem_opts *op
   if (!rc && (e = cudaMalloc(&v->s.redo, sizeof(int) * (size_t)max_cells)) != cudaSuccess)
     rc = cuda_fail(e, "cudaMalloc(solver)");
   if (!rc) v->s.redo_cap = (size_t)max_cells;
+  if (!rc && (e = cudaMalloc(&v->s.sm_limit, sizeof(int))) != cudaSuccess) rc = cuda_fail(e, "cudaMalloc(solver)");
+  if (!rc && (e = cudaHostAlloc(&v->h_words, 2 * sizeof(int), cudaHostAllocDefault)) != cudaSuccess)
+    rc = cuda_fail(e, "cudaHostAlloc(solver)");
+  if (!rc) {
+    v->h_words[0] = 1 << 20;
+    v->h_words[1] = 1 << 20;
+    if ((e = cudaMemcpy(v->s.sm_limit, v->h_words, sizeof(int), cudaMemcpyHostToDevice)) != cudaSuccess)
+      rc = cuda_fail(e, "cudaMemcpy(solver)");
+  }
   // scratch for a grid over every SM, so that pdr_solver_set_max_sms may widen it later
   pdr_chem_opts all = o;
   all.max_sms = 0;
@@ -395,8 +407,23 @@ int pdr_solver_run(pdr_solver *v, int ncell, double *d_abundance, const double *
     return PDR_E_ARG;
   }
   if (ncell == 0) return 0;
+  // a new run keeps every SM of its grid until pdr_solver_limit_sms says otherwise
+  cudaError_t e = cudaMemcpyAsync(v->s.sm_limit, v->h_words, sizeof(int), cudaMemcpyHostToDevice,
+                                  (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "pdr_solver_run: SM allowance");
   return solve_core(v->net, ncell, d_abundance, d_rate, d_density, d_t_end_yr, v->opts, d_status, d_stats, &v->s,
                     false, v->sms, (cudaStream_t)stream);
+}
+
+int pdr_solver_limit_sms(pdr_solver *v, int max_sms, void *control_stream) {
+  if (!v || max_sms < 1) {
+    set_error("pdr_solver_limit_sms: invalid argument");
+    return PDR_E_ARG;
+  }
+  v->h_words[1] = max_sms;
+  cudaError_t e = cudaMemcpyAsync(v->s.sm_limit, v->h_words + 1, sizeof(int), cudaMemcpyHostToDevice,
+                                  (cudaStream_t)control_stream);
+  return e == cudaSuccess ? 0 : cuda_fail(e, "pdr_solver_limit_sms");
 }
 
 int pdr_solver_set_max_sms(pdr_solver *v, int max_sms) {
@@ -413,6 +440,8 @@ void pdr_solver_free(pdr_solver *v) {
   if (v->s.counters) cudaFree(v->s.counters);
   if (v->s.redo) cudaFree(v->s.redo);
   if (v->s.cta) cudaFree(v->s.cta);
+  if (v->s.sm_limit) cudaFree(v->s.sm_limit);
+  if (v->h_words) cudaFreeHost(v->h_words);
   delete v;
 }
 

@@ -70,6 +70,8 @@ struct CtaArgs {
   int *fallback_list;
   int *fallback_count;
   int refill_static;
+  const int *sm_limit;    // work-queue mode: SMs the launch may keep (device word, null: all)
+  int grid_sms;           // SMs the grid was sized for
   double *kn_global;      // [gridDim.x][tab.nkn + 1] rate constants (times n_H where the RHS has it)
   void *mat_global;       // [gridDim.x][(n+2)*ld] Newton matrix, when it is not in shared memory
 };
@@ -701,7 +703,15 @@ __global__ void __launch_bounds__(256, 1) chem_cta_kernel(const __grid_constant_
     if (A.refill_static) {
       idx = blockIdx.x + k * gridDim.x;
     } else {
-      if (threadIdx.x == 0) next_idx = atomicAdd(A.queue, 1);
+      if (threadIdx.x == 0) {
+        // blocks beyond the launch's current SM allowance take no further cells
+        bool over = false;
+        if (A.sm_limit) {
+          const int lim = *reinterpret_cast<const volatile int *>(A.sm_limit);
+          over = (long long)blockIdx.x * A.grid_sms >= (long long)lim * gridDim.x;
+        }
+        next_idx = over ? 0x7fffffff : atomicAdd(A.queue, 1);
+      }
       __syncthreads();
       idx = next_idx;
       __syncthreads();
@@ -830,7 +840,7 @@ int chem_cta_blocks_per_sm(const pdr_net *net, bool mixed) {
 int launch_chem_cta(const pdr_net *net, int ncell, double *ab, const double *rate, const double *dens,
                     const double *tend, const pdr_chem_opts &o, int *status, int *stats, int *queue,
                     int *fb_list, int *fb_count, const int *cell_list, const int *total_ptr, bool mixed,
-                    int grid, void *scratch, cudaStream_t st) {
+                    int grid, void *scratch, cudaStream_t st, const int *sm_limit, int grid_sms) {
   const WarpTables &T = net->cta;
   if (!net->cta_ok || T.lanes > 256) return PDR_E_NET;
   CtaArgs A;
@@ -855,6 +865,8 @@ int launch_chem_cta(const pdr_net *net, int ncell, double *ab, const double *rat
   A.stats = stats;
   A.cell_list = cell_list;
   A.queue = queue;
+  A.sm_limit = sm_limit;
+  A.grid_sms = grid_sms > 0 ? grid_sms : 1;
   A.fallback_list = fb_list;
   A.fallback_count = fb_count;
   A.refill_static = (o.refill == 1 || (o.refill == 2 && !cell_list)) ? 1 : 0;

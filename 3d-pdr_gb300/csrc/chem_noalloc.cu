@@ -29,7 +29,7 @@ namespace pdr {
 int launch_chem_warp(const pdr_net *net, int ncell, double *ab, const double *rate, const double *dens,
                      const double *tend, const pdr_chem_opts &o, int *status, int *stats, int *queue,
                      int *fb_list, int *fb_count, const int *cell_list, const int *total_ptr, bool mixed,
-                     int sm_count, cudaStream_t st);
+                     int sm_count, cudaStream_t st, const int *sm_limit = nullptr);
 
 namespace {
 

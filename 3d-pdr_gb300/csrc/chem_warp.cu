@@ -58,7 +58,19 @@ struct ChemArgs {
   int *fallback_list;       // mixed mode: cells to redo in FP64
   int *fallback_count;
   int refill_static;        // 1: warp w takes cells w, w+W, ... ; 0: atomic work queue
+  // work-queue mode: SMs the launch may keep (device word, read between
+  // cells; null: all).  Blocks beyond limit * gridDim.x / grid_sms take no
+  // further cells, so a later launch on another stream gets their SMs.
+  const int *sm_limit;
+  int grid_sms;             // SMs the grid was sized for
 };
+
+// true when this block is beyond the launch's current SM allowance
+__device__ __forceinline__ bool over_sm_limit(const int *sm_limit, int grid_sms) {
+  if (!sm_limit) return false;
+  const int lim = *reinterpret_cast<const volatile int *>(sm_limit);
+  return (long long)blockIdx.x * grid_sms >= (long long)lim * gridDim.x;
+}
 
 // byte offsets of one warp's shared arrays (host and device agree)
 struct WarpLayout {
@@ -144,9 +156,6 @@ __device__ __forceinline__ bool lu_rows(MT *a, int ld, int lane, int &mystep, MT
     if (mystep < 0) {
       const MT l = row[k] * rinv;
       row[k] = l;
-#ifdef PDR_LU_SCALAR
-      for (int j = k + 1; j < N; j++) row[j] = fma(-l, prow[j], row[j]);
-#else
       // four columns at a time, every load before any store (the compiler
       // cannot tell the pivot row and this row apart)
       int j = k + 1;
@@ -159,7 +168,6 @@ __device__ __forceinline__ bool lu_rows(MT *a, int ld, int lane, int &mystep, MT
         row[j + 3] = fma(-l, p3, r3);
       }
       for (; j < N; j++) row[j] = fma(-l, prow[j], row[j]);
-#endif
     }
     __syncwarp();
   }
@@ -349,21 +357,6 @@ struct WarpCell : Core<WarpCell<NSP, MIXED, ZSH>, ZSH, MIXED> {
     if (owns)
       for (int j = 0; j < NSP + 2; j++) row[j] = MT(0);
     __syncwarp();
-#ifdef PDR_JAC_ROWS
-    if (owns) {
-      for (int t = 0; t < T.jac_len; t++) {
-        MT nu;
-        if constexpr (MIXED) nu = __ldg(&T.jac_nu_f[t * kWarp + lane]);
-        else nu = __ldg(&T.jac_nu[t * kWarp + lane]);
-        if (nu == MT(0)) break;
-        const int rab = __ldg(&T.jac_rab[t * kWarp + lane]);
-        const int r = rab & 0xffff, a = (rab >> 16) & 0xff, b = (rab >> 24) & 0xff;
-        row[a] = fma(nu, Da[r], row[a]);
-        row[b] = fma(nu, Db[r], row[b]);
-      }
-    }
-    __syncwarp();
-#else
     // term-parallel: the (row, column) contributions nu * dphi_r/dx_col sorted
     // by entry and cut into 32 balanced chunks; a lane sums each run of one
     // entry in a register and stores it, and a run that crosses a chunk
@@ -401,7 +394,6 @@ struct WarpCell : Core<WarpCell<NSP, MIXED, ZSH>, ZSH, MIXED> {
       }
       __syncwarp();
     }
-#endif
     const MT e = owns ? row[NSP] : MT(0);
     MT rf;
     if constexpr (MIXED) rf = (MT)rf_d * (wsc32 * this->atol32);   // row weight, normalised like the columns
@@ -517,7 +509,7 @@ __global__ void __launch_bounds__(RegVariant<RV>::threads, RegVariant<RV>::min_b
     if (A.refill_static) {
       idx = gwarp + k * nwarps;
     } else {
-      if (lane == 0) idx = atomicAdd(A.queue, 1);
+      if (lane == 0) idx = over_sm_limit(A.sm_limit, A.grid_sms) ? 0x7fffffff : atomicAdd(A.queue, 1);
       idx = __shfl_sync(FULL, idx, 0);
     }
     if (idx >= total_cells) break;
@@ -570,7 +562,7 @@ size_t chem_warp_smem_per_warp(const WarpTables &T, bool mixed, bool zshared) {
 int launch_chem_warp(const pdr_net *net, int ncell, double *ab, const double *rate, const double *dens,
                      const double *tend, const pdr_chem_opts &o, int *status, int *stats, int *queue,
                      int *fb_list, int *fb_count, const int *cell_list, const int *total_ptr, bool mixed,
-                     int sm_count, cudaStream_t st) {
+                     int sm_count, cudaStream_t st, const int *sm_limit) {
   const WarpTables &T = net->warp;
   if (T.neq != 32) return PDR_E_NET;
   ChemArgs A;
@@ -592,6 +584,8 @@ int launch_chem_warp(const pdr_net *net, int ncell, double *ab, const double *ra
   A.stats = stats;
   A.cell_list = cell_list;
   A.queue = queue;
+  A.sm_limit = sm_limit;
+  A.grid_sms = sm_count;
   A.fallback_list = fb_list;
   A.fallback_count = fb_count;
   // refill 2 (one warp per cell, no persistence) applies to the pass over

@@ -3,26 +3,33 @@
 // There is no counterpart in the reference: it is the service around the
 // chemistry path that a client calls with blocks of cells (physical
 // conditions plus initial abundances) and gets abundances back.  Design:
-//   * one lane per network: a dispatcher thread, a CUDA stream, a solver
-//     instance (pdr_solver, own scratch) and pinned staging plus device
-//     buffers for max_batch_cells cells, all allocated when the server is
-//     created -- nothing is allocated while serving;
-//   * FIFO admission with continuous batching: whenever a lane is free it
-//     takes every queued request of its network, in arrival order, that fits
-//     the remaining batch capacity, packs them into one launch (per-cell end
-//     times) and returns each request's cells when the launch completes;
-//   * lanes of different networks run concurrently on their own streams.  A
-//     persistent launch holds its SMs until its last cell is done, so by
-//     default a lane's launch spans every SM only when no other lane is
-//     running and an equal share with the running lanes otherwise
-//     (pdr_solver_set_max_sms).
+//   * one lane per network, each with slots_per_lane launch slots: a worker
+//     thread, a CUDA stream, a solver instance (pdr_solver, own scratch) and
+//     pinned staging plus device buffers for max_batch_cells cells, all
+//     allocated when the server is created -- nothing is allocated while
+//     serving;
+//   * continuous batching at slot level: a free slot takes every queued
+//     request of its network that fits its buffers, in arrival order, and runs
+//     them as one launch (rates, then the batched solve with per-cell end
+//     times); a request that arrives while other launches are on the GPU
+//     starts at once on another free slot, without waiting for them to drain;
+//   * SM sharing: persistent launches would hold their SMs until their last
+//     cell, so a new launch is sized for an equal share of the SMs with the
+//     launches in flight, and those are told to shrink to that share
+//     (pdr_solver_limit_sms, a 4-byte copy on a control stream): their blocks
+//     beyond it stop taking cells at the next cell boundary and the hardware
+//     hands those SMs to the new launch;
+//   * admission by device-memory footprint: requests whose bytes (inputs, rate
+//     constants, outputs per cell) would push the admitted-and-unfinished total
+//     over the budget are refused with PDR_E_BUSY.
 // Each cell is integrated independently, so a request's results do not depend
-// on what it was batched with.
+// on what it was batched or overlapped with.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <memory>
 #include <mutex>
 #include <thread>
 #include <unordered_map>
@@ -37,15 +44,14 @@ using Clock = std::chrono::steady_clock;
 struct Req {
   pdr_serve_request r;
   Clock::time_point submitted, finished;
+  double bytes = 0.0;
   bool done = false;
   int result = 0;
 };
 
-struct Lane {
-  pdr_net *net = nullptr;
+struct Slot {
   pdr_solver *solver = nullptr;
   cudaStream_t stream = nullptr;
-  int nspec = 0, nreac = 0;
   // pinned staging and device buffers, max_batch_cells cells each
   double *h_nH = nullptr, *h_T = nullptr, *h_Td = nullptr, *h_rad = nullptr, *h_AV = nullptr, *h_col = nullptr,
          *h_ab = nullptr, *h_tend = nullptr;
@@ -53,8 +59,17 @@ struct Lane {
   double *d_nH = nullptr, *d_T = nullptr, *d_Td = nullptr, *d_rad = nullptr, *d_AV = nullptr, *d_col = nullptr,
          *d_ab = nullptr, *d_tend = nullptr, *d_rate = nullptr;
   int *d_status = nullptr, *d_rstatus = nullptr;
-  std::deque<Req *> queue;
   std::thread thread;
+  bool running = false;
+  int share = 0;   // SMs this slot's launch may keep
+};
+
+struct Lane {
+  pdr_net *net = nullptr;
+  int nspec = 0, nreac = 0;
+  double cell_bytes = 0.0;
+  std::vector<std::unique_ptr<Slot>> slots;
+  std::deque<Req *> queue;
   long long batches = 0, cells = 0;
 };
 
@@ -63,99 +78,104 @@ struct Lane {
 struct pdr_server {
   pdr_phys phys;
   pdr_server_opts opts;
-  std::vector<Lane> lanes;
+  std::deque<Lane> lanes;   // (a deque: a Lane is not copyable)
   std::mutex mu;
   std::condition_variable work_cv, done_cv;
   bool stop = false;
   long long next_ticket = 1;
   std::unordered_map<long long, Req *> reqs;
   int device = 0, sms = 0;
-  int running = 0;   // lanes with a launch in flight
+  int running = 0;            // launches in flight
+  double admitted_bytes = 0.0, budget_bytes = 0.0;
+  cudaStream_t control = nullptr;   // the SM-allowance copies
 };
 
 namespace {
 
-int alloc_lane(pdr_server *s, Lane &L) {
+int alloc_slot(pdr_server *s, Lane &L, Slot &S) {
   const size_t n = (size_t)s->opts.max_batch_cells, nr = (size_t)s->opts.nrays;
   auto dev = [&](void **p, size_t bytes) { return cudaMalloc(p, bytes); };
   auto host = [&](void **p, size_t bytes) { return cudaHostAlloc(p, bytes, cudaHostAllocDefault); };
   cudaError_t e = cudaSuccess;
-  if ((e = host((void **)&L.h_nH, 8 * n)) || (e = host((void **)&L.h_T, 8 * n)) || (e = host((void **)&L.h_Td, 8 * n)) ||
-      (e = host((void **)&L.h_rad, 8 * n * nr)) || (e = host((void **)&L.h_AV, 8 * n * nr)) ||
-      (e = host((void **)&L.h_col, 8 * n * nr * 5)) || (e = host((void **)&L.h_ab, 8 * n * L.nspec)) ||
-      (e = host((void **)&L.h_tend, 8 * n)) || (e = host((void **)&L.h_status, 4 * n)))
+  if ((e = host((void **)&S.h_nH, 8 * n)) || (e = host((void **)&S.h_T, 8 * n)) || (e = host((void **)&S.h_Td, 8 * n)) ||
+      (e = host((void **)&S.h_rad, 8 * n * nr)) || (e = host((void **)&S.h_AV, 8 * n * nr)) ||
+      (e = host((void **)&S.h_col, 8 * n * nr * 5)) || (e = host((void **)&S.h_ab, 8 * n * L.nspec)) ||
+      (e = host((void **)&S.h_tend, 8 * n)) || (e = host((void **)&S.h_status, 4 * n)))
     return pdr::cuda_fail(e, "pdr_server_create: pinned staging");
-  if ((e = dev((void **)&L.d_nH, 8 * n)) || (e = dev((void **)&L.d_T, 8 * n)) || (e = dev((void **)&L.d_Td, 8 * n)) ||
-      (e = dev((void **)&L.d_rad, 8 * n * nr)) || (e = dev((void **)&L.d_AV, 8 * n * nr)) ||
-      (e = dev((void **)&L.d_col, 8 * n * nr * 5)) || (e = dev((void **)&L.d_ab, 8 * n * L.nspec)) ||
-      (e = dev((void **)&L.d_tend, 8 * n)) || (e = dev((void **)&L.d_rate, 8 * n * L.nreac)) ||
-      (e = dev((void **)&L.d_status, 4 * n)) || (e = dev((void **)&L.d_rstatus, 4 * n)))
+  if ((e = dev((void **)&S.d_nH, 8 * n)) || (e = dev((void **)&S.d_T, 8 * n)) || (e = dev((void **)&S.d_Td, 8 * n)) ||
+      (e = dev((void **)&S.d_rad, 8 * n * nr)) || (e = dev((void **)&S.d_AV, 8 * n * nr)) ||
+      (e = dev((void **)&S.d_col, 8 * n * nr * 5)) || (e = dev((void **)&S.d_ab, 8 * n * L.nspec)) ||
+      (e = dev((void **)&S.d_tend, 8 * n)) || (e = dev((void **)&S.d_rate, 8 * n * L.nreac)) ||
+      (e = dev((void **)&S.d_status, 4 * n)) || (e = dev((void **)&S.d_rstatus, 4 * n)))
     return pdr::cuda_fail(e, "pdr_server_create: device buffers");
-  if ((e = cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking)))
+  if ((e = cudaStreamCreateWithFlags(&S.stream, cudaStreamNonBlocking)))
     return pdr::cuda_fail(e, "pdr_server_create: stream");
-  return 0;
+  pdr_chem_opts o;
+  pdr_chem_opts_default(&o);
+  o.precision = s->opts.precision;
+  return pdr_solver_create(L.net, s->opts.max_batch_cells, &o, &S.solver);
 }
 
-void free_lane(Lane &L) {
-  for (void *p : {(void *)L.h_nH, (void *)L.h_T, (void *)L.h_Td, (void *)L.h_rad, (void *)L.h_AV, (void *)L.h_col,
-                  (void *)L.h_ab, (void *)L.h_tend, (void *)L.h_status})
+void free_slot(Slot &S) {
+  for (void *p : {(void *)S.h_nH, (void *)S.h_T, (void *)S.h_Td, (void *)S.h_rad, (void *)S.h_AV, (void *)S.h_col,
+                  (void *)S.h_ab, (void *)S.h_tend, (void *)S.h_status})
     if (p) cudaFreeHost(p);
-  for (void *p : {(void *)L.d_nH, (void *)L.d_T, (void *)L.d_Td, (void *)L.d_rad, (void *)L.d_AV, (void *)L.d_col,
-                  (void *)L.d_ab, (void *)L.d_tend, (void *)L.d_rate, (void *)L.d_status, (void *)L.d_rstatus})
+  for (void *p : {(void *)S.d_nH, (void *)S.d_T, (void *)S.d_Td, (void *)S.d_rad, (void *)S.d_AV, (void *)S.d_col,
+                  (void *)S.d_ab, (void *)S.d_tend, (void *)S.d_rate, (void *)S.d_status, (void *)S.d_rstatus})
     if (p) cudaFree(p);
-  if (L.solver) pdr_solver_free(L.solver);
-  if (L.stream) cudaStreamDestroy(L.stream);
+  if (S.solver) pdr_solver_free(S.solver);
+  if (S.stream) cudaStreamDestroy(S.stream);
 }
 
 // one launch over the packed requests: rates, then the batched solve
-int run_batch(pdr_server *s, Lane &L, const std::vector<Req *> &batch) {
+int run_batch(pdr_server *s, Lane &L, Slot &S, const std::vector<Req *> &batch) {
   const int nr = s->opts.nrays;
   size_t off = 0;
   for (Req *q : batch) {
     const pdr_serve_request &r = q->r;
     const size_t n = (size_t)r.ncell;
-    std::memcpy(L.h_nH + off, r.n_H, 8 * n);
-    std::memcpy(L.h_T + off, r.T, 8 * n);
-    std::memcpy(L.h_Td + off, r.Tdust, 8 * n);
-    std::memcpy(L.h_rad + off * nr, r.rad_surface, 8 * n * nr);
-    std::memcpy(L.h_AV + off * nr, r.AV, 8 * n * nr);
-    std::memcpy(L.h_col + off * nr * 5, r.column5, 8 * n * nr * 5);
-    std::memcpy(L.h_ab + off * L.nspec, r.abundance, 8 * n * L.nspec);
-    for (size_t i = 0; i < n; i++) L.h_tend[off + i] = r.t_end_yr;
+    std::memcpy(S.h_nH + off, r.n_H, 8 * n);
+    std::memcpy(S.h_T + off, r.T, 8 * n);
+    std::memcpy(S.h_Td + off, r.Tdust, 8 * n);
+    std::memcpy(S.h_rad + off * nr, r.rad_surface, 8 * n * nr);
+    std::memcpy(S.h_AV + off * nr, r.AV, 8 * n * nr);
+    std::memcpy(S.h_col + off * nr * 5, r.column5, 8 * n * nr * 5);
+    std::memcpy(S.h_ab + off * L.nspec, r.abundance, 8 * n * L.nspec);
+    for (size_t i = 0; i < n; i++) S.h_tend[off + i] = r.t_end_yr;
     off += n;
   }
   const int n = (int)off;
-  cudaStream_t st = L.stream;
+  cudaStream_t st = S.stream;
   cudaError_t e = cudaSuccess;
   auto h2d = [&](void *d, const void *h, size_t bytes) {
     if (e == cudaSuccess) e = cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, st);
   };
-  h2d(L.d_nH, L.h_nH, 8 * (size_t)n);
-  h2d(L.d_T, L.h_T, 8 * (size_t)n);
-  h2d(L.d_Td, L.h_Td, 8 * (size_t)n);
-  h2d(L.d_rad, L.h_rad, 8 * (size_t)n * nr);
-  h2d(L.d_AV, L.h_AV, 8 * (size_t)n * nr);
-  h2d(L.d_col, L.h_col, 8 * (size_t)n * nr * 5);
-  h2d(L.d_ab, L.h_ab, 8 * (size_t)n * L.nspec);
-  h2d(L.d_tend, L.h_tend, 8 * (size_t)n);
+  h2d(S.d_nH, S.h_nH, 8 * (size_t)n);
+  h2d(S.d_T, S.h_T, 8 * (size_t)n);
+  h2d(S.d_Td, S.h_Td, 8 * (size_t)n);
+  h2d(S.d_rad, S.h_rad, 8 * (size_t)n * nr);
+  h2d(S.d_AV, S.h_AV, 8 * (size_t)n * nr);
+  h2d(S.d_col, S.h_col, 8 * (size_t)n * nr * 5);
+  h2d(S.d_ab, S.h_ab, 8 * (size_t)n * L.nspec);
+  h2d(S.d_tend, S.h_tend, 8 * (size_t)n);
   if (e != cudaSuccess) return pdr::cuda_fail(e, "pdr_server: host-to-device copy");
-  int rc = pdr_rates_batched(L.net, &s->phys, n, nr, L.d_T, L.d_Td, L.d_rad, L.d_AV, L.d_col, L.d_rate, L.d_rstatus,
+  int rc = pdr_rates_batched(L.net, &s->phys, n, nr, S.d_T, S.d_Td, S.d_rad, S.d_AV, S.d_col, S.d_rate, S.d_rstatus,
                              st);
   if (rc) return rc;
-  rc = pdr_solver_run(L.solver, n, L.d_ab, L.d_rate, L.d_nH, L.d_tend, L.d_status, nullptr, st);
+  rc = pdr_solver_run(S.solver, n, S.d_ab, S.d_rate, S.d_nH, S.d_tend, S.d_status, nullptr, st);
   if (rc) return rc;
-  if ((e = cudaMemcpyAsync(L.h_ab, L.d_ab, 8 * (size_t)n * L.nspec, cudaMemcpyDeviceToHost, st)) ||
-      (e = cudaMemcpyAsync(L.h_status, L.d_status, 4 * (size_t)n, cudaMemcpyDeviceToHost, st)) ||
+  if ((e = cudaMemcpyAsync(S.h_ab, S.d_ab, 8 * (size_t)n * L.nspec, cudaMemcpyDeviceToHost, st)) ||
+      (e = cudaMemcpyAsync(S.h_status, S.d_status, 4 * (size_t)n, cudaMemcpyDeviceToHost, st)) ||
       (e = cudaStreamSynchronize(st)))
     return pdr::cuda_fail(e, "pdr_server: device-to-host copy");
   off = 0;
   for (Req *q : batch) {
     const size_t m = (size_t)q->r.ncell;
-    std::memcpy(q->r.abundance, L.h_ab + off * L.nspec, 8 * m * L.nspec);
+    std::memcpy(q->r.abundance, S.h_ab + off * L.nspec, 8 * m * L.nspec);
     int res = 0;
     for (size_t i = 0; i < m; i++) {
-      if (q->r.status) q->r.status[i] = L.h_status[off + i];
-      if (L.h_status[off + i] != 0) res = L.h_status[off + i];
+      if (q->r.status) q->r.status[i] = S.h_status[off + i];
+      if (S.h_status[off + i] != 0) res = S.h_status[off + i];
     }
     q->result = res;
     off += m;
@@ -163,8 +183,25 @@ int run_batch(pdr_server *s, Lane &L, const std::vector<Req *> &batch) {
   return 0;
 }
 
-void lane_loop(pdr_server *s, int li) {
+// Called with the server lock held: the SMs of a launch that is about to
+// start, and the shrinking of the launches in flight to the same share.
+int claim_sms(pdr_server *s, Slot &me) {
+  if (!s->opts.partition_sms) return 0;
+  const int share = std::max(1, s->sms / (s->running + 1));
+  for (Lane &L : s->lanes)
+    for (auto &sp : L.slots) {
+      Slot &o = *sp;
+      if (&o == &me || !o.running || o.share <= share) continue;
+      o.share = share;
+      pdr_solver_limit_sms(o.solver, share, s->control);
+    }
+  me.share = share;
+  return share;
+}
+
+void slot_loop(pdr_server *s, int li, int si) {
   Lane &L = s->lanes[li];
+  Slot &S = *L.slots[si];
   cudaSetDevice(s->device);
   for (;;) {
     std::vector<Req *> batch;
@@ -178,21 +215,22 @@ void lane_loop(pdr_server *s, int li) {
         batch.push_back(L.queue.front());
         L.queue.pop_front();
       }
-      // SM share of this launch: all SMs when the other lanes are idle, else
-      // an equal share with the lanes that are running
-      if (s->opts.partition_sms && s->lanes.size() > 1)
-        pdr_solver_set_max_sms(L.solver, s->running == 0 ? 0 : std::max(1, s->sms / (s->running + 1)));
+      const int share = claim_sms(s, S);
+      pdr_solver_set_max_sms(S.solver, share);
+      S.running = true;
       s->running++;
     }
-    const int rc = run_batch(s, L, batch);
+    const int rc = run_batch(s, L, S, batch);
     const Clock::time_point t = Clock::now();
     {
       std::lock_guard<std::mutex> lk(s->mu);
       s->running--;
+      S.running = false;
       for (Req *q : batch) {
         if (rc) q->result = rc;
         q->finished = t;
         q->done = true;
+        s->admitted_bytes -= q->bytes;
         L.cells += q->r.ncell;
       }
       L.batches++;
@@ -211,6 +249,8 @@ void pdr_server_opts_default(pdr_server_opts *o) {
   o->nrays = 12;
   o->precision = PDR_MIXED;
   o->partition_sms = 1;
+  o->slots_per_lane = 4;
+  o->hbm_budget_mb = 0.0;
 }
 
 int pdr_server_create(pdr_net *const *nets, int nnet, const pdr_phys *phys, const pdr_server_opts *opts,
@@ -224,7 +264,8 @@ int pdr_server_create(pdr_net *const *nets, int nnet, const pdr_phys *phys, cons
   s->phys = *phys;
   pdr_server_opts_default(&s->opts);
   if (opts) s->opts = *opts;
-  if (s->opts.max_batch_cells <= 0 || s->opts.nrays <= 0) {
+  if (s->opts.max_batch_cells <= 0 || s->opts.nrays <= 0 || s->opts.slots_per_lane < 1 ||
+      s->opts.slots_per_lane > 64 || !(s->opts.hbm_budget_mb >= 0.0)) {
     delete s;
     pdr::set_error("pdr_server_create: invalid options");
     return PDR_E_ARG;
@@ -233,42 +274,65 @@ int pdr_server_create(pdr_net *const *nets, int nnet, const pdr_phys *phys, cons
   cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, s->device);
   s->lanes.resize(nnet);
   int rc = 0;
+  cudaError_t e = cudaStreamCreateWithFlags(&s->control, cudaStreamNonBlocking);
+  if (e != cudaSuccess) rc = pdr::cuda_fail(e, "pdr_server_create: control stream");
+  double capacity = 0.0;
+  const double nr = s->opts.nrays;
   for (int i = 0; i < nnet && !rc; i++) {
     Lane &L = s->lanes[i];
     L.net = nets[i];
     if (!L.net) { rc = PDR_E_ARG; pdr::set_error("pdr_server_create: null network"); break; }
     L.nspec = L.net->host.nspec;
     L.nreac = L.net->host.nreac;
-    rc = alloc_lane(s, L);
-    if (rc) break;
-    pdr_chem_opts o;
-    pdr_chem_opts_default(&o);
-    o.precision = s->opts.precision;
-    rc = pdr_solver_create(L.net, s->opts.max_batch_cells, &o, &L.solver);
+    // device bytes per cell: n_H, T, T_dust, end time, per-ray field, A_V and
+    // five columns, abundances, rate constants, two status words
+    L.cell_bytes = 8.0 * (4 + 7 * nr + L.nspec + L.nreac) + 8.0;
+    for (int k = 0; k < s->opts.slots_per_lane && !rc; k++) {
+      L.slots.emplace_back(new Slot());
+      rc = alloc_slot(s, L, *L.slots.back());
+    }
+    capacity += L.cell_bytes * s->opts.max_batch_cells * s->opts.slots_per_lane;
   }
-  // one warm-up cell per lane: kernel attributes and device tables are set up
+  s->budget_bytes = s->opts.hbm_budget_mb > 0.0 ? s->opts.hbm_budget_mb * 1048576.0 : capacity;
+  // one warm-up cell per slot: kernel attributes and device tables are set up
   // now, not inside the first request's latency
   for (int i = 0; i < nnet && !rc; i++) {
     Lane &L = s->lanes[i];
-    const int nr = s->opts.nrays;
-    std::vector<double> ab(L.nspec, 1e-20);
-    ab[0] = 1.0;
-    pdr_serve_request r{};
-    r.network = i; r.ncell = 1; r.t_end_yr = 1.0;
-    std::vector<double> nH(1, 1e3), T(1, 50.0), Td(1, 15.0), rad(nr, 1.0), AV(nr, 1.0), col(nr * 5, 1e15);
-    r.n_H = nH.data(); r.T = T.data(); r.Tdust = Td.data(); r.rad_surface = rad.data(); r.AV = AV.data();
-    r.column5 = col.data(); r.abundance = ab.data(); r.status = nullptr;
-    Req q;
-    q.r = r;
-    rc = run_batch(s, L, {&q});
+    const int nrays = s->opts.nrays;
+    for (auto &sp : L.slots) {
+      if (rc) break;
+      std::vector<double> ab(L.nspec, 1e-20);
+      ab[0] = 1.0;
+      pdr_serve_request r{};
+      r.network = i; r.ncell = 1; r.t_end_yr = 1.0;
+      std::vector<double> nH(1, 1e3), T(1, 50.0), Td(1, 15.0), rad(nrays, 1.0), AV(nrays, 1.0), col(nrays * 5, 1e15);
+      r.n_H = nH.data(); r.T = T.data(); r.Tdust = Td.data(); r.rad_surface = rad.data(); r.AV = AV.data();
+      r.column5 = col.data(); r.abundance = ab.data(); r.status = nullptr;
+      Req q;
+      q.r = r;
+      rc = run_batch(s, L, *sp, {&q});
+    }
   }
   if (rc) {
-    for (Lane &L : s->lanes) free_lane(L);
+    for (Lane &L : s->lanes)
+      for (auto &sp : L.slots) free_slot(*sp);
+    if (s->control) cudaStreamDestroy(s->control);
     delete s;
     return rc;
   }
-  for (int i = 0; i < nnet; i++) s->lanes[i].thread = std::thread(lane_loop, s, i);
+  for (int i = 0; i < nnet; i++)
+    for (int k = 0; k < (int)s->lanes[i].slots.size(); k++)
+      s->lanes[i].slots[k]->thread = std::thread(slot_loop, s, i, k);
   *out = s;
+  return 0;
+}
+
+int pdr_server_footprint(pdr_server *s, int network, int ncell, double *bytes) {
+  if (!s || !bytes || network < 0 || network >= (int)s->lanes.size() || ncell < 0) {
+    pdr::set_error("pdr_server_footprint: invalid argument");
+    return PDR_E_ARG;
+  }
+  *bytes = s->lanes[network].cell_bytes * ncell;
   return 0;
 }
 
@@ -279,11 +343,21 @@ int pdr_server_submit(pdr_server *s, const pdr_serve_request *r, long long *tick
     pdr::set_error("pdr_server_submit: invalid request (ncell above max_batch_cells?)");
     return PDR_E_ARG;
   }
+  const double bytes = s->lanes[r->network].cell_bytes * r->ncell;
   Req *q = new Req();
   q->r = *r;
+  q->bytes = bytes;
   q->submitted = Clock::now();
   {
     std::lock_guard<std::mutex> lk(s->mu);
+    // admission by footprint; a request alone above the budget is still
+    // admitted when nothing else is, so that it can ever run
+    if (s->admitted_bytes > 0.0 && s->admitted_bytes + bytes > s->budget_bytes) {
+      delete q;
+      pdr::set_error("pdr_server_submit: the request would exceed the device-memory budget; retry later");
+      return PDR_E_BUSY;
+    }
+    s->admitted_bytes += bytes;
     *ticket = s->next_ticket++;
     s->reqs[*ticket] = q;
     s->lanes[r->network].queue.push_back(q);
@@ -325,9 +399,12 @@ void pdr_server_free(pdr_server *s) {
   }
   s->work_cv.notify_all();
   for (Lane &L : s->lanes)
-    if (L.thread.joinable()) L.thread.join();
-  for (Lane &L : s->lanes) free_lane(L);
+    for (auto &sp : L.slots)
+      if (sp->thread.joinable()) sp->thread.join();
+  for (Lane &L : s->lanes)
+    for (auto &sp : L.slots) free_slot(*sp);
   for (auto &kv : s->reqs) delete kv.second;
+  if (s->control) cudaStreamDestroy(s->control);
   delete s;
 }
 

@@ -32,7 +32,14 @@ class ChemOpts(C.Structure):
 
 class ServerOpts(C.Structure):
     _fields_ = [("max_batch_cells", C.c_int), ("nrays", C.c_int), ("precision", C.c_int),
-                ("partition_sms", C.c_int)]
+                ("partition_sms", C.c_int), ("slots_per_lane", C.c_int), ("hbm_budget_mb", C.c_double)]
+
+
+PDR_E_BUSY = -1005
+
+
+class Busy(RuntimeError):
+    """The server refused a request that would exceed its device-memory budget now."""
 
 
 class ServeRequest(C.Structure):
@@ -128,6 +135,8 @@ def lib():
     L.pdr_server_wait.argtypes = [_vp, C.c_longlong, C.POINTER(C.c_double)]
     L.pdr_server_stats.argtypes = [_vp, C.c_int, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
     L.pdr_server_free.argtypes = [_vp]
+    L.pdr_server_footprint.argtypes = [_vp, C.c_int, C.c_int, C.POINTER(C.c_double)]
+    L.pdr_solver_limit_sms.argtypes = [_vp, C.c_int, _vp]
     _LIB = L
     return L
 
@@ -394,15 +403,20 @@ class Solver:
 
 
 class Server:
-    """The serving loop (pdr_server_*): one lane per network, FIFO continuous
-    batching, everything allocated up front.  Requests are numpy arrays that
-    must stay alive until wait() returns (the object keeps references)."""
+    """The serving loop (pdr_server_*): one lane per network with several launch
+    slots, continuous batching, SM sharing between launches in flight, admission
+    by device-memory footprint, everything allocated up front.  Requests are
+    numpy arrays that must stay alive until wait() returns (the object keeps
+    references)."""
 
-    def __init__(self, nets, ph, max_batch_cells=65536, nrays=12, precision="mixed"):
+    def __init__(self, nets, ph, max_batch_cells=65536, nrays=12, precision="mixed", slots_per_lane=4,
+                 hbm_budget_mb=0.0, partition_sms=True):
         o = ServerOpts()
         lib().pdr_server_opts_default(C.byref(o))
         o.max_batch_cells, o.nrays = max_batch_cells, nrays
         o.precision = PDR_MIXED if precision == "mixed" else PDR_FP64
+        o.slots_per_lane, o.hbm_budget_mb = slots_per_lane, hbm_budget_mb
+        o.partition_sms = 1 if partition_sms else 0
         arr = (_vp * len(nets))(*[n.handle for n in nets])
         h = _vp()
         check(lib().pdr_server_create(arr, len(nets), C.byref(ph), C.byref(o), C.byref(h)), "pdr_server_create")
@@ -416,7 +430,10 @@ class Server:
         r = ServeRequest(network, len(arrs[0]), float(t_end_yr), *[a.ctypes.data for a in arrs],
                          abundance.ctypes.data, status.ctypes.data if status is not None else None)
         t = C.c_longlong()
-        check(lib().pdr_server_submit(self.handle, C.byref(r), C.byref(t)), "pdr_server_submit")
+        rc = lib().pdr_server_submit(self.handle, C.byref(r), C.byref(t))
+        if rc == PDR_E_BUSY:
+            raise Busy(lib().pdr_last_error().decode())
+        check(rc, "pdr_server_submit")
         self._keep[t.value] = (arrs, abundance, status, r)
         return t.value
 
@@ -426,6 +443,12 @@ class Server:
         rc = lib().pdr_server_wait(self.handle, ticket, C.byref(lat))
         self._keep.pop(ticket, None)
         return rc, lat.value
+
+    def footprint(self, network, ncell):
+        """Device bytes a request of ncell cells of that network takes while admitted."""
+        b = C.c_double()
+        check(lib().pdr_server_footprint(self.handle, network, ncell, C.byref(b)), "pdr_server_footprint")
+        return b.value
 
     def stats(self, lane):
         b, c = C.c_longlong(), C.c_longlong()

@@ -112,27 +112,51 @@ int pdr_solver_run(pdr_solver *solver, int ncell, double *d_abundance, const dou
                    void *stream);
 /* limit the persistent grid of later runs to max_sms SMs' worth of blocks (0: all) */
 int pdr_solver_set_max_sms(pdr_solver *solver, int max_sms);
+/* Shrink the run of this instance that is in flight (or the next one, if it
+ * starts after the copy) to max_sms SMs' worth of blocks: the blocks beyond
+ * that take no further cells once they finish their current one, and the
+ * remaining cells go to the blocks that stay, so another instance launched on
+ * another stream gets those SMs within one cell's integration time.  The value
+ * is written by a 4-byte copy on control_stream, which must not be the run's
+ * own stream (the copy would wait for the run).  Each pdr_solver_run starts
+ * again with every SM of its grid.  Results do not depend on the allowance.
+ * Work-queue mode (refill 0) only; no counterpart in the reference. */
+int pdr_solver_limit_sms(pdr_solver *solver, int max_sms, void *control_stream);
 void pdr_solver_free(pdr_solver *solver);
 
 /* ---- serving (no counterpart in the reference) ----
- * A server owns one lane per network (a dispatcher thread, a stream, a solver
- * instance, pinned staging and device buffers for max_batch_cells cells, all
- * allocated by pdr_server_create).  Requests are blocks of cells given by
- * their physical conditions and initial abundances; each lane serves its
- * network's requests in arrival order, packing every queued request that fits
- * into one launch (reaction rates, then the batched solve, per-cell end
- * times).  The arrays of a request must stay valid until pdr_server_wait
- * returns for its ticket; abundance[ncell*nspec] is overwritten with the
- * result and status[ncell] (or NULL) receives the cells' CVODE flags. */
+ * A server owns one lane per network, and each lane slots_per_lane launch
+ * slots: a worker thread, a stream, a solver instance, pinned staging and
+ * device buffers for max_batch_cells cells, all allocated by
+ * pdr_server_create (nothing is allocated while serving).  Requests are blocks
+ * of cells given by their physical conditions and initial abundances.  A free
+ * slot takes every queued request of its network that fits, in arrival order,
+ * and runs them as one launch (reaction rates, then the batched solve with
+ * per-cell end times), so requests that arrive while other launches are on
+ * the GPU start at once on another slot.  With partition_sms the SMs are
+ * shared: a new launch takes an equal share with the launches in flight, and
+ * those shrink to that share at their next cell boundary
+ * (pdr_solver_limit_sms), so no launch waits for another to drain.  Admission
+ * is by device-memory footprint: a request whose cells (inputs, rate
+ * constants, outputs) would take the bytes of the requests admitted and not
+ * yet finished above hbm_budget_mb is refused with PDR_E_BUSY, to be retried.
+ * The arrays of a request must stay valid until pdr_server_wait returns for
+ * its ticket; abundance[ncell*nspec] is overwritten with the result and
+ * status[ncell] (or NULL) receives the cells' CVODE flags.  Each cell is
+ * integrated on its own, so a request's results do not depend on the others
+ * in flight. */
+#define PDR_E_BUSY -1005   /* server: the request would exceed the memory budget now */
 typedef struct pdr_server pdr_server;
 typedef struct {
-  int max_batch_cells;  /* cells per launch per lane, also the largest request (65536) */
+  int max_batch_cells;  /* cells per launch, also the largest request (65536)         */
   int nrays;            /* rays per cell in the requests (12)                           */
   int precision;        /* PDR_MIXED (default) or PDR_FP64                              */
-  int partition_sms;    /* 1 (default): a lane's launch spans every SM when no other
-                           lane is running, else an equal share with the running
-                           lanes, so that one network's persistent launch does not hold
-                           every SM while another network waits; 0: all SMs always */
+  int partition_sms;    /* 1 (default): launches in flight share the SMs equally (see
+                           above); 0: every launch is sized for all SMs and the
+                           hardware shares them                                        */
+  int slots_per_lane;   /* launches in flight per network (4)                           */
+  double hbm_budget_mb; /* device-memory footprint of the admitted, unfinished requests
+                           (0: what the slots' buffers hold)                           */
 } pdr_server_opts;
 typedef struct {
   int network;          /* index into the server's network list                        */
@@ -152,6 +176,8 @@ int pdr_server_submit(pdr_server *server, const pdr_serve_request *request, long
  * a PDR_E_* code; latency_ms (or NULL) receives submit-to-completion time */
 int pdr_server_wait(pdr_server *server, long long ticket, double *latency_ms);
 int pdr_server_stats(pdr_server *server, int lane, long long *batches, long long *cells);
+/* bytes of device memory a request of ncell cells of that network takes while admitted */
+int pdr_server_footprint(pdr_server *server, int network, int ncell, double *bytes);
 void pdr_server_free(pdr_server *server);
 
 /* Allocation-free variant of pdr_chem_solve_batched, with no counterpart in
