@@ -18,6 +18,8 @@
 //   (cells that fail the check are re-solved in FP64, status 2); negative
 //   populations are set to zero.
 #include <algorithm>
+#include <mutex>
+#include <vector>
 
 #include "pdr_internal.h"
 
@@ -28,10 +30,29 @@ constexpr double KB = 1.38065040e-16, CL = 2.99792458e+10, HP = 6.62606896e-27;
 constexpr double PI = 3.141592653589793238462643383279502884197;
 constexpr unsigned FULL = 0xffffffffu;
 
-// per-warp shared memory: two nlev^2 FP64 matrices, four nlev vectors, three int vectors
-__host__ __device__ inline size_t levpop_warp_bytes(int n) {
+// per-warp shared memory: the nlev^2 FP64 rate matrix, the line values of the
+// radiative pairs, four nlev vectors, three int vectors and, for the mixed
+// solve, an nlev^2 FP32 matrix and an nlev FP32 vector
+struct LevLayout {
+  size_t R, lines, b, sp, x, rs, ipiv, indxr, indxc, Mf, total;
+};
+__host__ __device__ inline LevLayout levpop_layout(int n, int nrad, bool mixed) {
   auto al = [](size_t v) { return (v + 15) & ~size_t(15); };
-  return al(8 * (size_t)n * n) * 2 + al(8 * (size_t)n) * 4 + al(4 * (size_t)n) * 3;
+  LevLayout L;
+  size_t o = 0;
+  L.R = o; o += al(8 * (size_t)n * n);
+  L.lines = o; o += al(8 * (size_t)(nrad > 0 ? nrad : 1));
+  L.b = o; o += al(8 * (size_t)n);
+  L.sp = o; o += al(8 * (size_t)n);
+  L.x = o; o += al(8 * (size_t)n);
+  L.rs = o; o += al(8 * (size_t)n);
+  L.ipiv = o; o += al(4 * (size_t)n);
+  L.indxr = o; o += al(4 * (size_t)n);
+  L.indxc = o; o += al(4 * (size_t)n);
+  L.Mf = o;
+  if (mixed) o += al(4 * (size_t)n * n) + al(4 * (size_t)n);
+  L.total = o;
+  return L;
 }
 
 struct LevArgs {
@@ -147,24 +168,35 @@ __device__ bool gauss_jordan(R *a, R *b, int n, R *dumv, int *indxr, int *indxc,
   return true;
 }
 
+// The mixed solve's acceptance test on the correction s that a further
+// refinement step would make to population x: above 1e-6 of the coolant
+// density it must be below 1e-7 of x, above 1e-12 of the density below 1e-4
+// of x (ten times inside the 1e-6 and 1e-3 the results are held to), and it
+// must contract (at most half the previous correction, or negligible)
+__device__ __forceinline__ bool refine_ok(double ax, double as, double prev, double dens) {
+  const bool contracts = as <= 0.5 * prev || as <= 1.0e-12 * ax;
+  if (ax > 1.0e-6 * dens) return as <= 1.0e-7 * ax && contracts;
+  if (ax > 1.0e-12 * dens) return as <= 1.0e-4 * ax && contracts;
+  return true;
+}
+
 template <bool MIXED>
 __global__ void __launch_bounds__(256) levpop_kernel(const __grid_constant__ CoolantTables C,
                                                      const __grid_constant__ LevArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int n = C.nlev, nn = n * n;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  auto al = [](size_t v) { return (v + 15) & ~size_t(15); };
-  const size_t per_warp = levpop_warp_bytes(n);
-  unsigned char *base = smem + per_warp * warp;
-  double *R = reinterpret_cast<double *>(base);              // rates, then the solvlevpop matrix
-  double *aux = reinterpret_cast<double *>(base + al(8 * nn)); // line values, then FP32 matrix
-  double *b = reinterpret_cast<double *>(base + 2 * al(8 * nn));
-  double *sp = b + al(8 * n) / 8;
-  double *x = sp + al(8 * n) / 8;
-  double *rs = x + al(8 * n) / 8;    // row scales of the FP32 solve
-  int *ipiv = reinterpret_cast<int *>(reinterpret_cast<unsigned char *>(rs) + al(8 * n));
-  int *indxr = ipiv + al(4 * n) / 4;
-  int *indxc = indxr + al(4 * n) / 4;
+  const LevLayout L = levpop_layout(n, C.nrad, MIXED);
+  unsigned char *base = smem + L.total * warp;
+  double *R = reinterpret_cast<double *>(base + L.R);          // rates, then the solvlevpop matrix
+  double *lines = reinterpret_cast<double *>(base + L.lines);  // line values of the radiative pairs
+  double *b = reinterpret_cast<double *>(base + L.b);
+  double *sp = reinterpret_cast<double *>(base + L.sp);
+  double *x = reinterpret_cast<double *>(base + L.x);
+  double *rs = reinterpret_cast<double *>(base + L.rs);        // row scales of the FP32 solve
+  int *ipiv = reinterpret_cast<int *>(base + L.ipiv);
+  int *indxr = reinterpret_cast<int *>(base + L.indxr);
+  int *indxc = reinterpret_cast<int *>(base + L.indxc);
   const int wpb = blockDim.x >> 5;
   for (int cell = blockIdx.x * wpb + warp; cell < A.ncell; cell += gridDim.x * wpb) {
     const double T = A.T[cell], Td = A.Td[cell], rho = A.density[cell];
@@ -189,12 +221,12 @@ __global__ void __launch_bounds__(256) levpop_kernel(const __grid_constant__ Coo
       const double step = (klo == khi) ? 0.0 : (T - tp[klo - 1]) / (tp[khi - 1] - tp[klo - 1]);
       const double *lo = C.col + ((size_t)q * C.ntemp + (klo - 1)) * nn;
       const double *hi = C.col + ((size_t)q * C.ntemp + (khi - 1)) * nn;
+      const double dsingle = (p == 0 ? nH2 : p == 3 ? ne : p == 4 ? nH : p == 5 ? nHe : nHp);
       for (int e = lane; e < nn; e += 32) {
         const double tmp = lo[e] + (hi[e] - lo[e]) * step;
         double add;
-        if (p == 1) add = tmp * nH2 * fpara;
-        else if (p == 2) add = tmp * nH2 * fortho;
-        else add = tmp * (p == 0 ? nH2 : p == 3 ? ne : p == 4 ? nH : p == 5 ? nHe : nHp);
+        if (p == 1 || p == 2) add = tmp * nH2 * (p == 1 ? fpara : fortho);
+        else add = tmp * dsingle;
         R[e] = R[e] + add;
       }
     }
@@ -202,8 +234,6 @@ __global__ void __launch_bounds__(256) levpop_kernel(const __grid_constant__ Coo
     // ---- escape probabilities and the radiative terms ----
     const double ngrain = 2.0e-12 * rho * A.metallicity * 100. / A.g2d;
     const double *tau = A.tau + (size_t)cell * C.nlin * A.nrays;
-    for (int e = lane; e < nn; e += 32) aux[e] = 0.0;
-    __syncwarp();
     // pairs with no radiative coupling in either direction (A = B = 0) leave
     // R unchanged and their line term zero: only the radiative pairs are visited
     for (int pe = lane; pe < C.nrad; pe += 32) {
@@ -240,7 +270,7 @@ __global__ void __launch_bounds__(256) levpop_kernel(const __grid_constant__ Coo
           beta = A.pseudo1d ? bsum : bsum / (double)A.nrays;
         }
       }
-      if (has_line) aux[e] = Aij * HP * f * sp[i] * beta * (S - bb) / S;
+      lines[pe] = has_line ? Aij * HP * f * sp[i] * beta * (S - bb) / S : 0.0;
       const double field = (1.0 - beta) * S + beta * bb;
       const int et = j * n + i;
       R[e] = (Aij + C.B[e] * field) + R[e];
@@ -249,15 +279,21 @@ __global__ void __launch_bounds__(256) levpop_kernel(const __grid_constant__ Coo
     __syncwarp();
     for (int e = lane; e < nn; e += 32)
       if (fabs(R[e]) < 1.0e-50) R[e] = 0.0;
-    __syncwarp();
+    // the cooling rate: the line values summed over i > j in row-major order,
+    // as the reference adds them; the non-radiative pairs contribute zeros,
+    // which leave the sum unchanged, so only the radiative pairs are added
     if (lane == 0) {
       double cool = 0.0;
-      for (int i = 0; i < n; i++)
-        for (int j = 0; j < i; j++) cool = cool + aux[i * n + j];
+      for (int pe = 0; pe < C.nrad; pe++) cool = cool + lines[pe];
       A.cooling[cell] = cool;
     }
-    if (A.line)
-      for (int e = lane; e < nn; e += 32) A.line[(size_t)cell * nn + e] = aux[e];
+    if (A.line) {
+      double *lo = A.line + (size_t)cell * nn;
+      for (int e = lane; e < nn; e += 32) lo[e] = 0.0;
+      __syncwarp();
+      for (int pe = lane; pe < C.nrad; pe += 32) lo[C.rad_pairs[pe]] = lines[pe];
+    }
+    __syncwarp();
     // ---- solvlevpop matrix: transpose, diagonal -sum, conservation row ----
     for (int i = lane; i < n; i += 32) {
       double out = 0.0;
@@ -283,8 +319,11 @@ __global__ void __launch_bounds__(256) levpop_kernel(const __grid_constant__ Coo
       for (int i = lane; i < n; i += 32) x[i] = b[i];
     } else {
       // rows equilibrated by their largest entry, FP32 Gauss-Jordan inverse of
-      // D M, then x = inv D b and one FP64 refinement x += inv D (b - M x)
-      float *Mf = reinterpret_cast<float *>(aux);
+      // D M, then x = inv D b and up to two FP64 refinement steps
+      // x += inv D (b - M x), each accepted by the size of the correction the
+      // next step would make (refine_ok); otherwise the cell is re-solved by
+      // the FP64 Gauss-Jordan (R is intact)
+      float *Mf = reinterpret_cast<float *>(base + L.Mf);
       float *bf = Mf + nn;
       for (int i = lane; i < n; i += 32) {
         double mx = 0.0;
@@ -302,41 +341,30 @@ __global__ void __launch_bounds__(256) levpop_kernel(const __grid_constant__ Coo
         for (int l = 0; l < n; l++) s = fma((double)Mf[i * n + l], rs[l] * b[l], s);
         x[i] = s;
       }
-      __syncwarp();
-      for (int i = lane; i < n; i += 32) {
-        double s = b[i];
-        for (int l = 0; l < n; l++) s = fma(-R[i * n + l], x[l], s);
-        sp[i] = s * rs[i];   // scaled residual (s_pop is no longer needed)
+      bool good = false;
+      for (int it = 0; it < 3 && ok && !good; it++) {
+        __syncwarp();
+        for (int i = lane; i < n; i += 32) {
+          double s = b[i];
+          for (int l = 0; l < n; l++) s = fma(-R[i * n + l], x[l], s);
+          sp[i] = s * rs[i];   // scaled residual (s_pop is no longer needed)
+        }
+        __syncwarp();
+        bool bad = false;
+        for (int i = lane; i < n; i += 32) {
+          double s = 0.0;
+          for (int l = 0; l < n; l++) s = fma((double)Mf[i * n + l], sp[l], s);
+          // from the second correction on, the correction is also the test of
+          // the previous one
+          if (it > 0 && !refine_ok(fabs(x[i]), fabs(s), (double)bf[i], dens)) bad = true;
+          if (it < 2) {
+            x[i] += s;
+            bf[i] = (float)fabs(s);
+          }
+        }
+        good = (it > 0) && !__any_sync(FULL, bad);
       }
-      __syncwarp();
-      for (int i = lane; i < n; i += 32) {
-        double s = 0.0;
-        for (int l = 0; l < n; l++) s = fma((double)Mf[i * n + l], sp[l], s);
-        x[i] += s;
-        bf[i] = (float)fabs(s);   // size of the first correction
-      }
-      __syncwarp();
-      // verify with the correction a second refinement would make: for every
-      // population above 1e-14 of the coolant density it must be below 1e-8
-      // of the population and at most half of the first correction (the
-      // refinement contracts, so the remaining error is bounded by it);
-      // otherwise the cell is re-solved by the FP64 Gauss-Jordan (R is intact)
-      for (int i = lane; i < n; i += 32) {
-        double s = b[i];
-        for (int l = 0; l < n; l++) s = fma(-R[i * n + l], x[l], s);
-        sp[i] = s * rs[i];
-      }
-      __syncwarp();
-      bool bad = false;
-      for (int i = lane; i < n; i += 32) {
-        double s = 0.0;
-        for (int l = 0; l < n; l++) s = fma((double)Mf[i * n + l], sp[l], s);
-        const double ax = fabs(x[i]), as = fabs(s);
-        const bool small = as <= 1.0e-8 * ax;
-        const bool contracts = as <= 0.5 * (double)bf[i] || as <= 1.0e-12 * ax;
-        if (ax > 1.0e-14 * dens && !(small && contracts)) bad = true;
-      }
-      if (!ok || __any_sync(FULL, bad)) {
+      if (!ok || !good) {
         __syncwarp();
         for (int i = lane; i < n; i += 32) b[i] = 0.0;
         __syncwarp();
@@ -360,7 +388,7 @@ __global__ void __launch_bounds__(256) levpop_kernel(const __grid_constant__ Coo
 
 }  // namespace
 
-size_t levpop_smem_per_warp(int n) { return levpop_warp_bytes(n); }
+size_t levpop_smem_per_warp(int n, int nrad, bool mixed) { return levpop_layout(n, nrad, mixed).total; }
 
 namespace {
 // LTE populations of one cell per thread: CALCULATE_PARTITION_FUNCTION and
@@ -403,28 +431,54 @@ int launch_levpop(const pdr_coolant *c, const LevArgsHost &h, bool mixed, int sm
     set_error("pdr_levpop_batched: coolants with more than 64 levels are not supported");
     return PDR_E_ARG;
   }
-  const size_t pw = levpop_smem_per_warp(n);
-  int wpb = (int)((96 * 1024) / pw);
-  if (wpb > 8) wpb = 8;
-  if (wpb < 1) wpb = 1;
-  const size_t smem = pw * wpb;
-  cudaError_t e;
-  int per_sm = 0;
-  if (mixed) {
-    e = cudaFuncSetAttribute(levpop_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(levpop)");
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, levpop_kernel<true>, wpb * 32, smem);
-  } else {
-    e = cudaFuncSetAttribute(levpop_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(levpop)");
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, levpop_kernel<false>, wpb * 32, smem);
+  // the FP32 inverse with refinement pays off only for larger systems: the
+  // 5-level coolants take the FP64 elimination in both forms
+  if (n <= 8) mixed = false;
+  const size_t pw = levpop_smem_per_warp(n, c->dev.nrad, mixed);
+  // the block size (1..8 warps) that keeps the most warps resident per SM
+  // (the shared memory of one warp bounds it for the 41-level coolant),
+  // chosen once per device and warp size; the attribute is set to the largest
+  // candidate and never lowered, so concurrent launches cannot undercut it
+  auto kern = mixed ? levpop_kernel<true> : levpop_kernel<false>;
+  int dev = 0, optin = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  struct Shape { int dev; size_t pw; bool mixed; int wpb, per_sm; };
+  static std::mutex mu;
+  static std::vector<Shape> shapes;
+  static size_t attr[64][2] = {};
+  int wpb = 0, per_sm = 0;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    for (const Shape &sh : shapes)
+      if (sh.dev == dev && sh.pw == pw && sh.mixed == mixed) { wpb = sh.wpb; per_sm = sh.per_sm; }
+    if (wpb == 0) {
+      const size_t top = std::min((size_t)optin, pw * 8);
+      if (top > attr[dev & 63][mixed]) {
+        e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)top);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(levpop)");
+        attr[dev & 63][mixed] = top;
+      }
+      for (int w = 8; w >= 1; w--) {
+        if (pw * w > top) continue;
+        int b = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, w * 32, pw * w);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor(levpop)");
+        if (b * w > per_sm * wpb) { wpb = w; per_sm = b; }
+      }
+      if (wpb < 1) {
+        set_error("pdr_levpop_batched: one warp's shared memory exceeds a block's");
+        return PDR_E_ARG;
+      }
+      shapes.push_back({dev, pw, mixed, wpb, per_sm});
+    }
   }
-  if (per_sm < 1) per_sm = 1;
+  const size_t smem = pw * wpb;
   long long blocks = ((long long)h.ncell + wpb - 1) / wpb;
   if (blocks > (long long)sm_count * per_sm) blocks = (long long)sm_count * per_sm;
   if (blocks < 1) blocks = 1;
-  if (mixed) levpop_kernel<true><<<(int)blocks, wpb * 32, smem, st>>>(c->dev, A);
-  else levpop_kernel<false><<<(int)blocks, wpb * 32, smem, st>>>(c->dev, A);
+  kern<<<(int)blocks, wpb * 32, smem, st>>>(c->dev, A);
   e = cudaGetLastError();
   return e == cudaSuccess ? 0 : cuda_fail(e, "levpop_kernel launch");
 }

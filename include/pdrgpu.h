@@ -255,10 +255,12 @@ int pdr_net_special_reactions(const pdr_net *net, int nr[6]);
  * d_cooling[ncell] (the coolant's cooling_rate), d_line[ncell*nlev*nlev] or
  * NULL, d_status[ncell] (0 ok, 1 singular matrix, 2 mixed solve re-done in
  * FP64) or NULL.  precision PDR_FP64 solves with the reference's full-pivot
- * Gauss-Jordan; PDR_MIXED uses a row-equilibrated FP32 Gauss-Jordan inverse
- * plus one FP64 iterative-refinement step, and re-solves in FP64 the cells
- * whose next correction would exceed 1e-7 of a population above 1e-12 of the
- * coolant density. */
+ * Gauss-Jordan; PDR_MIXED uses, for coolants of more than 8 levels, a
+ * row-equilibrated FP32 Gauss-Jordan inverse plus up to two FP64
+ * iterative-refinement steps, accepted when the next correction is below 1e-7
+ * of every population above 1e-6 of the coolant density and below 1e-4 of
+ * those above 1e-12, and shrinking; other cells are re-solved in FP64 (status
+ * 2).  Coolants of up to 8 levels take the FP64 solve in both forms. */
 int pdr_coolant_load(const char *path, int nlev, int ntemp, pdr_coolant **out);
 void pdr_coolant_free(pdr_coolant *c);
 int pdr_coolant_info(const pdr_coolant *c, int *nlev, int *nlin);
