@@ -49,11 +49,17 @@ struct CoefShared {
   double tau[QMAX + 2];
   double l[QMAX + 1];
   double rl1;     // 1/l[1]
-  // coefficients of a uniform step history (xi_j = j), per order 1..5
+  double tqd[6];
+  float tqf[6], tauf[QMAX + 2];
+};
+
+// coefficients of a uniform step history (xi_j = j), per order 1..5: the
+// same for every integrator, so one copy serves a whole block
+struct CoefUniform {
   double ul[QMAX + 1][QMAX + 1];
   double url1[QMAX + 1];
-  double tqd[6], utqd[QMAX + 1][6];
-  float tqf[6], utqf[QMAX + 1][6], tauf[QMAX + 2];
+  double utqd[QMAX + 1][6];
+  float utqf[QMAX + 1][6];
 };
 
 // Comparisons of uniform FP64 scalars in integer arithmetic: for operands
@@ -136,6 +142,7 @@ struct Core {
   using NT = typename std::conditional<NORM32, float, double>::type;
   __device__ __forceinline__ D &self() { return *static_cast<D *>(this); }
   CoefShared *ws = nullptr;
+  CoefUniform *wu = nullptr;   // the uniform-history table (may be shared by several integrators)
   // Nordsieck row of this thread's species, weight, correction, work values
   typename std::conditional<ZSHARED, ZShared, ZRow>::type z;
   NT ewt;
@@ -156,8 +163,8 @@ struct Core {
     else return ws->tqd;
   }
   __device__ __forceinline__ NT utqn(int qq, int j) const {
-    if constexpr (NORM32) return ws->utqf[qq][j];
-    else return ws->utqd[qq][j];
+    if constexpr (NORM32) return wu->utqf[qq][j];
+    else return wu->utqd[qq][j];
   }
   __device__ __forceinline__ const NT *taun() const {
     if constexpr (NORM32) return ws->tauf;
@@ -347,11 +354,11 @@ struct Core {
       coeffs<double>(qq, true, 1.0, one, l, tq);
       self().sync();
       if (self().leader()) {
-        for (int j = 0; j <= QMAX; j++) ws->ul[qq][j] = l[j];
-        ws->url1[qq] = 1.0 / l[1];
+        for (int j = 0; j <= QMAX; j++) wu->ul[qq][j] = l[j];
+        wu->url1[qq] = 1.0 / l[1];
         for (int j = 1; j <= 5; j++) {
-          ws->utqd[qq][j] = tq[j];
-          ws->utqf[qq][j] = (float)tq[j];
+          wu->utqd[qq][j] = tq[j];
+          wu->utqf[qq][j] = (float)tq[j];
         }
       }
     }
@@ -380,8 +387,8 @@ struct Core {
       else h_nt = h;
       if (self().leader()) {
 #pragma unroll
-        for (int j = 0; j <= QMAX; j++) ws->l[j] = ws->ul[q][j];
-        ws->rl1 = ws->url1[q];
+        for (int j = 0; j <= QMAX; j++) ws->l[j] = wu->ul[q][j];
+        ws->rl1 = wu->url1[q];
         tq[2] = utqn(q, 2);
         tq[4] = utqn(q, 4);
         tq[5] = utqn(q, 5);

@@ -78,7 +78,7 @@ struct CtaArgs {
 
 // byte offsets of the block's shared arrays (host and device agree)
 struct CtaLayout {
-  size_t scr, xs, part, red, sig, perm, cols, bsv, ys, upan, ws, mat, total;
+  size_t scr, xs, part, red, sig, perm, cols, bsv, ys, upan, ws, wu, mat, total;
 };
 
 __host__ __device__ inline size_t al16(size_t x) { return (x + 15) & ~size_t(15); }
@@ -101,6 +101,7 @@ __host__ __device__ inline CtaLayout cta_layout(const WarpTables &T, int ld, siz
   L.ys = o; o += al16(mt * (size_t)(n + DB));
   L.upan = o; o += al16(mt * PB * (size_t)n);
   L.ws = o; o += al16(sizeof(CoefShared));
+  L.wu = o; o += al16(sizeof(CoefUniform));
   L.mat = o;
   if (mat_smem) o += al16(mt * (size_t)(n + 2) * ld);
   L.total = o;
@@ -226,8 +227,12 @@ struct CtaCell : Core<CtaCell<MIXED>, false, MIXED> {
     if (tid == 0) kn[T.nkn] = 0.0;
     __syncthreads();
     for (int e = tid; e < T.nkext; e += blockDim.x) {
-      const int2 q = __ldg(&T.kext[e]);
-      kn[T.nreac + e] = (double)q.y * kn[q.x];
+      double k = 0.0;
+      for (int q = __ldg(&T.kext_ptr[e]); q < __ldg(&T.kext_ptr[e + 1]); q++) {
+        const int2 rn = __ldg(&T.kext_rn[q]);
+        k = fma((double)rn.y, kn[rn.x], k);
+      }
+      kn[T.nreac + e] = k;
     }
   }
 
@@ -693,6 +698,7 @@ __global__ void __launch_bounds__(256, 1) chem_cta_kernel(const __grid_constant_
   c.ys = reinterpret_cast<MT *>(smem_raw + L.ys);
   c.upan = reinterpret_cast<MT *>(smem_raw + L.upan);
   c.ws = reinterpret_cast<CoefShared *>(smem_raw + L.ws);
+  c.wu = reinterpret_cast<CoefUniform *>(smem_raw + L.wu);
   c.mat = mat_smem ? reinterpret_cast<MT *>(smem_raw + L.mat)
                    : reinterpret_cast<MT *>(A.mat_global) + (size_t)blockIdx.x * (A.n + 2) * A.ld;
   c.build_uniform_table();
@@ -750,6 +756,7 @@ __global__ void __launch_bounds__(256, 1) eval_cta_kernel(const __grid_constant_
   c.ys = reinterpret_cast<double *>(smem_raw + L.ys);
   c.upan = reinterpret_cast<double *>(smem_raw + L.upan);
   c.ws = reinterpret_cast<CoefShared *>(smem_raw + L.ws);
+  c.wu = reinterpret_cast<CoefUniform *>(smem_raw + L.wu);
   c.mat = mat_smem ? reinterpret_cast<double *>(smem_raw + L.mat)
                    : reinterpret_cast<double *>(A.mat_global) + (size_t)blockIdx.x * (n + 2) * A.ld;
   c.rtol = A.reltol;

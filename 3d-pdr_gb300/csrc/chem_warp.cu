@@ -88,7 +88,7 @@ __host__ __device__ inline WarpLayout warp_layout(int nsp, const WarpTables &T, 
   L.scr = o; o += al(scr);
   L.xs = o; o += al(8 * (size_t)(nsp + 2));
   L.part = o; o += al(8 * (size_t)(T.nparts + 1));
-  L.jrow = o; o += al((mixed ? 4 : 8) * (size_t)nsp * (nsp + 3));
+  L.jrow = o; o += al((mixed ? 4 : 8) * (size_t)nsp * (nsp + 1));
   L.sig = o; o += al(4 * (size_t)(nsp + 2) + 4 * (size_t)nsp + 4 * (size_t)(nsp + 2));   // sig, perm, xs32
   L.ws = o; o += al(sizeof(CoefShared) + (zsh ? 8 * (QMAX + 1) * kWarp : 0));
   L.total = o;
@@ -200,6 +200,9 @@ __device__ __forceinline__ MT lu_solve_rows(const MT *a, int ld, int lane, int m
 template <int NSP, bool MIXED, bool ZSH>
 struct WarpCell : Core<WarpCell<NSP, MIXED, ZSH>, ZSH, MIXED> {
   using MT = typename std::conditional<MIXED, float, double>::type;
+  // Newton-matrix row stride: the species columns and the x_e column (odd, so
+  // the rows of a warp fall in distinct banks)
+  static constexpr int LDJ = NSP + 1;
   const ChemArgs &A;
   const int lane;
   const bool owns;
@@ -266,8 +269,12 @@ struct WarpCell : Core<WarpCell<NSP, MIXED, ZSH>, ZSH, MIXED> {
     }
     __syncwarp();
     for (int e = lane; e < T.nkext; e += kWarp) {
-      const int2 q = __ldg(&T.kext[e]);
-      kn[T.nreac + e] = (double)q.y * kn[q.x];
+      double k = 0.0;
+      for (int q = __ldg(&T.kext_ptr[e]); q < __ldg(&T.kext_ptr[e + 1]); q++) {
+        const int2 rn = __ldg(&T.kext_rn[q]);
+        k = fma((double)rn.y, kn[rn.x], k);
+      }
+      kn[T.nreac + e] = k;
     }
     __syncwarp();
   }
@@ -353,9 +360,9 @@ struct WarpCell : Core<WarpCell<NSP, MIXED, ZSH>, ZSH, MIXED> {
         Db[r] = (ab.y == NSP + 1) ? 0.0 : k * xs[ab.x];
       }
     }
-    MT *row = jrow + lane * (NSP + 3);
+    MT *row = jrow + lane * (LDJ);
     if (owns)
-      for (int j = 0; j < NSP + 2; j++) row[j] = MT(0);
+      for (int j = 0; j < LDJ; j++) row[j] = MT(0);
     __syncwarp();
     // term-parallel: the (row, column) contributions nu * dphi_r/dx_col sorted
     // by entry and cut into 32 balanced chunks; a lane sums each run of one
@@ -378,7 +385,7 @@ struct WarpCell : Core<WarpCell<NSP, MIXED, ZSH>, ZSH, MIXED> {
         s = fma(nu, (x & 0x10000) ? Db[r] : Da[r], s);
         const int kind = (x >> 17) & 3;
         if (kind == 1) {
-          jrow[(y & 0xff) * (NSP + 3) + ((y >> 8) & 0xff)] = s;
+          jrow[(y & 0xff) * (LDJ) + ((y >> 8) & 0xff)] = s;
           s = MT(0);
         } else if (kind == 2) {
           slots[y >> 16] = s;
@@ -390,7 +397,7 @@ struct WarpCell : Core<WarpCell<NSP, MIXED, ZSH>, ZSH, MIXED> {
         const int tt = __ldg(&T.bnd_t[b]), ss = __ldg(&T.bnd_s[b]);
         MT acc = MT(0);
         for (int q = ss & 0xffff; q < (ss >> 16); q++) acc += slots[q];
-        jrow[(tt & 0xff) * (NSP + 3) + ((tt >> 8) & 0xff)] = acc;
+        jrow[(tt & 0xff) * (LDJ) + ((tt >> 8) & 0xff)] = acc;
       }
       __syncwarp();
     }
@@ -413,8 +420,8 @@ struct WarpCell : Core<WarpCell<NSP, MIXED, ZSH>, ZSH, MIXED> {
   __device__ __forceinline__ bool setup(double yv) {
     assemble(yv, -this->gamma, true);
     __syncwarp();
-    const bool ok = lu_rows<NSP, MT>(jrow, NSP + 3, lane, mystep, invd, perm);
-    const MT *row = jrow + lane * (NSP + 3);
+    const bool ok = lu_rows<NSP, MT>(jrow, LDJ, lane, mystep, invd, perm);
+    const MT *row = jrow + lane * (LDJ);
     bool finite = true;
     if (owns)
       for (int j = 0; j < NSP; j++) finite &= isfinite(row[j]);
@@ -424,7 +431,7 @@ struct WarpCell : Core<WarpCell<NSP, MIXED, ZSH>, ZSH, MIXED> {
   }
 
   __device__ __forceinline__ double solve(double b) {
-    const double x = lu_solve_rows<NSP, double>(jrow, NSP + 3, lane, mystep, invd, b, perm);
+    const double x = lu_solve_rows<NSP, double>(jrow, LDJ, lane, mystep, invd, b, perm);
     return owns ? x : 0.0;
   }
 
@@ -432,7 +439,7 @@ struct WarpCell : Core<WarpCell<NSP, MIXED, ZSH>, ZSH, MIXED> {
   // scaling of the FP32 matrix), the correction comes back times ssc*gscale,
   // in FP32 for the norm and in FP64 for the state
   __device__ __forceinline__ double solve32(double b, float gs, float &x32) {
-    const float xv = lu_solve_rows<NSP, float>(jrow, NSP + 3, lane, mystep, invd, (float)b * wsc32, perm);
+    const float xv = lu_solve_rows<NSP, float>(jrow, LDJ, lane, mystep, invd, (float)b * wsc32, perm);
     x32 = owns ? xv * (ssc32 * gs) : 0.0f;
     return (double)x32;
   }
@@ -501,7 +508,11 @@ __global__ void __launch_bounds__(RegVariant<RV>::threads, RegVariant<RV>::min_b
     c.z.p = reinterpret_cast<double *>(reinterpret_cast<unsigned char *>(c.ws) + sizeof(CoefShared)) + lane;
     c.z.s = kWarp;
   }
-  c.build_uniform_table();
+  // the uniform-history coefficient table, one copy per block
+  __shared__ CoefUniform uni;
+  c.wu = &uni;
+  if (warp == 0) c.build_uniform_table();
+  __syncthreads();
   if (total_ptr) total_cells = *total_ptr;
   const int gwarp = blockIdx.x * (blockDim.x >> 5) + warp, nwarps = gridDim.x * (blockDim.x >> 5);
   for (int k = 0;; k++) {
@@ -545,7 +556,7 @@ __global__ void __launch_bounds__(128) eval_kernel(const __grid_constant__ ChemA
       c.assemble(yv, 1.0, false);
       if (lane < NSP)
 #pragma unroll
-        for (int j = 0; j < NSP; j++) out[((size_t)s * NSP + lane) * NSP + j] = c.jrow[lane * (NSP + 3) + j];
+        for (int j = 0; j < NSP; j++) out[((size_t)s * NSP + lane) * NSP + j] = c.jrow[lane * WarpCell<NSP, false, false>::LDJ + j];
     }
     __syncwarp();
   }

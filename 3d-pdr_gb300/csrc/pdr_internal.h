@@ -41,13 +41,15 @@ struct WarpTables {
   // RHS f_i = sum over terms of (nu kn_r) * operand: operands are the slot
   // values (0..neq+1) and the products x_a x_b of the distinct two-body
   // reactant pairs (neq+2 ..); the rate constants kn[0..nkn) are the per-cell
-  // kn_r followed by the extras |nu| kn_r of the terms with |nu| > 1, and
-  // kn[nkn] is a constant zero for the padding terms
+  // kn_r followed by the extras: the coefficient sum_r nu_r kn_r of the terms
+  // of one species that share an operand, or nu kn_r of a single term with
+  // |nu| > 1; kn[nkn] is a constant zero for the padding terms
   int nkn = 0, nkext = 0, npairs = 0, nop = 0;
   int2 *rhs_t = nullptr;      // [rhs_len][lanes] (kn index | (partial slot written after the term + 1) << 16,
                               //  operand | sign of nu << 31)
   int2 *pairs = nullptr;      // [npairs] slots (a, b) of each reactant pair
-  int2 *kext = nullptr;       // [nkext] (reaction, |nu|) of each extra rate constant
+  int *kext_ptr = nullptr;    // [nkext+1] extra rate constant e = sum over kext_rn[kext_ptr[e]..kext_ptr[e+1])
+  int2 *kext_rn = nullptr;    //   of nu * kn_r, (reaction r, nu) in reaction order
   int *plist = nullptr;       // [plist_len][lanes] partial slots of species `lane`
   int *jac_rab = nullptr;     // [jac_len][lanes] reaction | slot a << 16 | slot b << 24
   double *jac_nu = nullptr;   // [jac_len][lanes]

@@ -8,6 +8,7 @@
 // tables the kernels read: reactant slots per reaction, the net stoichiometry as
 // per-species term lists, and their balanced split over the 32 lanes of a warp.
 #include <algorithm>
+#include <limits>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -238,7 +239,7 @@ int build_device_tables(pdr_net *net) {
   // the packed term tables hold a reaction in 16 bits and a slot in 8: larger
   // networks get no integrator tables (the solve entry points reject them)
   if (h.nreac >= 65536 || neq + 2 > 255) return rc;
-  auto build = [&](int G, WarpTables &w) -> int {
+  auto build = [&](int G, WarpTables &w, size_t max_merged) -> int {
     w.neq = neq;
     w.nreac = h.nreac;
     w.lanes = G;
@@ -267,49 +268,93 @@ int build_device_tables(pdr_net *net) {
         op_of[r] = ab.x;
       }
     }
-    std::map<std::pair<int, int>, int> ext_index;
-    std::vector<int2> kext;   // (reaction, |nu|) of the extra constants
-    auto kidx_of = [&](int r, double nu) {
-      const int m = (int)std::fabs(nu);
-      if (m == 1) return r;
-      auto it = ext_index.find({r, m});
-      if (it == ext_index.end()) {
-        it = ext_index.emplace(std::make_pair(r, m), (int)kext.size()).first;
-        kext.push_back(make_int2(r, m));
-      }
-      return h.nreac + it->second;
-    };
     for (auto &t : terms)
       if (std::fabs(t.nu) != std::floor(std::fabs(t.nu)) || std::fabs(t.nu) > 64) return PDR_E_NET;
-    // the sorted term list cut into G balanced chunks; a chunk flushes its
+    // Terms of one species that share an operand (reactions with the same
+    // reactants and different products) are merged: their coefficient
+    // sum_r nu_r kn_r is formed once per cell as an extra rate constant
+    // (kn[nreac + e], summed in reaction order), so the RHS takes one FMA for
+    // them.  A single term with nu = +-1 reads kn_r with the sign bit flipped;
+    // any other single term reads an extra constant nu kn_r.
+    struct MTerm { int i, op, kidx; bool neg; };
+    std::vector<MTerm> mt;
+    std::vector<int> kext_ptr(1, 0);
+    std::vector<int2> kext_rn;   // (reaction, nu) of the extras' summands
+    auto extra = [&](const std::vector<int> &ts) {
+      for (int t : ts) kext_rn.push_back(make_int2(terms[t].r, (int)terms[t].nu));
+      kext_ptr.push_back((int)kext_rn.size());
+      return h.nreac + (int)kext_ptr.size() - 2;
+    };
+    // the groups of terms (one species, one operand), in species order and
+    // operand order of first appearance
+    struct Group { int i, op; std::vector<int> ts; };
+    std::vector<Group> groups;
+    for (int t0 = 0; t0 < T;) {
+      const int i = terms[t0].i;
+      int t1 = t0;
+      while (t1 < T && terms[t1].i == i) t1++;
+      std::map<int, int> at;
+      for (int t = t0; t < t1; t++) {
+        const int op = op_of[terms[t].r];
+        auto it = at.find(op);
+        if (it == at.end()) {
+          at[op] = (int)groups.size();
+          groups.push_back({i, op, {t}});
+        } else {
+          groups[it->second].ts.push_back(t);
+        }
+      }
+      t0 = t1;
+    }
+    // every extra rate constant costs 8 bytes of a warp integrator's shared
+    // memory: the largest groups are merged first, up to max_merged of them
+    std::vector<int> by_size;
+    for (int g = 0; g < (int)groups.size(); g++)
+      if (groups[g].ts.size() > 1) by_size.push_back(g);
+    std::stable_sort(by_size.begin(), by_size.end(),
+                     [&](int a, int b) { return groups[a].ts.size() > groups[b].ts.size(); });
+    std::vector<char> merge(groups.size(), 0);
+    for (size_t k = 0; k < by_size.size() && k < max_merged; k++) merge[by_size[k]] = 1;
+    for (int g = 0; g < (int)groups.size(); g++) {
+      const Group &gr = groups[g];
+      if (merge[g]) {
+        mt.push_back({gr.i, gr.op, extra(gr.ts), false});
+        continue;
+      }
+      for (int t : gr.ts) {
+        if (std::fabs(terms[t].nu) == 1.0) mt.push_back({gr.i, gr.op, terms[t].r, terms[t].nu < 0});
+        else mt.push_back({gr.i, gr.op, extra({t}), false});
+      }
+    }
+    const int M = (int)mt.size();
+    // the merged term list cut into G balanced chunks; a chunk flushes its
     // running sum into a partial slot whenever the species changes
-    w.rhs_len = std::max(1, (T + G - 1) / G);
-    std::vector<int2> rt(w.rhs_len * G, make_int2(0, ONE));   // padding: 0 * x_one
+    w.rhs_len = std::max(1, (M + G - 1) / G);
+    std::vector<int2> rt(w.rhs_len * G, make_int2(0, ONE));
     std::vector<std::vector<int>> parts(G);
     int slot = 0;
     for (int l = 0; l < G; l++) {
-      int b = l * w.rhs_len, e = std::min(T, b + w.rhs_len);
+      int b = l * w.rhs_len, e = std::min(M, b + w.rhs_len);
       for (int t = b; t < e; t++) {
         int k = t - b, fl = -1;
-        if (t + 1 == e || terms[t + 1].i != terms[t].i) {
+        if (t + 1 == e || mt[t + 1].i != mt[t].i) {
           fl = slot;
-          parts[terms[t].i].push_back(slot);
+          parts[mt[t].i].push_back(slot);
           slot++;
         }
-        const int kidx = kidx_of(terms[t].r, terms[t].nu);
-        rt[k * G + l] = make_int2(kidx | ((fl + 1) << 16),
-                                  op_of[terms[t].r] | (terms[t].nu < 0 ? (int)0x80000000u : 0));
+        rt[k * G + l] = make_int2(mt[t].kidx | ((fl + 1) << 16), mt[t].op | (mt[t].neg ? (int)0x80000000u : 0));
       }
     }
     // padding terms read the constant-zero rate slot nkn (kn is zero-filled there)
-    const int nkn = h.nreac + (int)kext.size();
+    const int nkext = (int)kext_ptr.size() - 1;
+    const int nkn = h.nreac + nkext;
     for (int l = 0; l < G; l++) {
-      int b = l * w.rhs_len, e = std::min(T, b + w.rhs_len);
+      int b = l * w.rhs_len, e = std::min(M, b + w.rhs_len);
       for (int t = std::max(e, b); t < b + w.rhs_len; t++) rt[(t - b) * G + l] = make_int2(nkn, ONE);
     }
     if (slot + 1 >= 65536 || nkn + 1 >= 65536) return PDR_E_NET;
     w.nkn = nkn;
-    w.nkext = (int)kext.size();
+    w.nkext = nkext;
     w.npairs = (int)pairs.size();
     w.nop = neq + 2 + w.npairs;
     w.nparts = slot;
@@ -400,7 +445,8 @@ int build_device_tables(pdr_net *net) {
     w.nh_mask = upload(net, nhm, rc2);
     w.rhs_t = upload(net, rt, rc2);
     w.pairs = upload(net, pairs, rc2);
-    w.kext = upload(net, kext, rc2);
+    w.kext_ptr = upload(net, kext_ptr, rc2);
+    w.kext_rn = upload(net, kext_rn, rc2);
     w.plist = upload(net, pl, rc2);
     w.jac_rab = upload(net, jr, rc2);
     w.jac_nu = upload(net, jn, rc2);
@@ -419,13 +465,16 @@ int build_device_tables(pdr_net *net) {
     return rc2;
   };
   if (neq <= kWarp) {
-    const int e = build(kWarp, net->warp);
+    // a warp integrator keeps its rate constants in shared memory: at most 96
+    // merged groups keep the mixed form at 16 warps per SM
+    const int e = build(kWarp, net->warp, 96);
     if (e) rc = e;
     net->warp_ok = (e == 0);
   }
   {
     const int G = std::max(64, (neq + kWarp - 1) / kWarp * kWarp);
-    const int e = build(G, net->cta);
+    // the block integrator keeps its rate constants in global memory
+    const int e = build(G, net->cta, std::numeric_limits<size_t>::max());
     if (e) rc = e;
     net->cta_ok = (e == 0);
   }
