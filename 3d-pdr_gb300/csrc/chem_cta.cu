@@ -78,13 +78,17 @@ struct CtaArgs {
 
 // byte offsets of the block's shared arrays (host and device agree)
 struct CtaLayout {
-  size_t scr, xs, part, red, sig, perm, cols, bsv, ys, upan, ws, wu, mat, total;
+  size_t scr, xs, part, red, sig, perm, cols, bsv, ys, upan, ws, wu, mat, dinv, yv, rfs, idx, wv, total;
 };
 
 __host__ __device__ inline size_t al16(size_t x) { return (x + 15) & ~size_t(15); }
 
-__host__ __device__ inline CtaLayout cta_layout(const WarpTables &T, int ld, size_t mt, bool mat_smem) {
-  const int n = T.neq, nreac = T.nreac, nparts = T.nparts, G = T.lanes;
+// sp: the mixed form's sparse Newton matrix (storage of T.sp.total values,
+// the dense routines on its m x m trailing block)
+__host__ __device__ inline CtaLayout cta_layout(const WarpTables &T, int ld, size_t mt, bool mat_smem,
+                                                bool sp = false) {
+  const int nreac = T.nreac, nparts = T.nparts, G = T.lanes;
+  const int n = sp ? T.sp.m : T.neq;   // order of the dense matrix
   CtaLayout L;
   size_t o = 0;
   // scr: the RHS operands (FP64) or the two Jacobian scatter buffers
@@ -94,16 +98,31 @@ __host__ __device__ inline CtaLayout cta_layout(const WarpTables &T, int ld, siz
   L.xs = o; o += al16(8 * (size_t)(n + 2));
   L.part = o; o += al16(8 * (size_t)(nparts + 1));
   L.red = o; o += al16(2 * MAXW * (8 + 8 + 4));   // sums, argmax keys, argmax rows
-  L.sig = o; o += al16(4 * (size_t)(n + 2) * 2);   // column scales, then the FP32 slot values
+  L.sig = o; o += al16(4 * (size_t)(T.neq + 2) * 2);   // column scales, then the FP32 slot values
   L.perm = o; o += al16(4 * (size_t)n);
   L.cols = o; o += al16(4 * (size_t)(n + MAXW));   // nonzero U columns of a panel, per-warp counts
   L.bsv = o; o += al16(mt * (size_t)G);
   L.ys = o; o += al16(mt * (size_t)(n + DB));
-  L.upan = o; o += al16(mt * PB * (size_t)n);
+  // LU panel; also the assembly's boundary slots (at most 2G - 2)
+  L.upan = o; o += al16(mt * (size_t)(PB * n > 2 * G ? PB * n : 2 * G));
   L.ws = o; o += al16(sizeof(CoefShared));
   L.wu = o; o += al16(sizeof(CoefUniform));
   L.mat = o;
-  if (mat_smem) o += al16(mt * (size_t)(n + 2) * ld);
+  if (sp) {
+    o += al16(mt * (size_t)T.sp.total);
+    L.dinv = o; o += al16(mt * (size_t)(T.sp.a > 0 ? T.sp.a : 1));
+    L.yv = o; o += al16(mt * (size_t)T.sp.N);
+    L.rfs = o; o += al16(4 * (size_t)T.sp.N);
+    // the index tables (a_col, b_col, a_ptr, a_diag, b_ptr, iperm, ul_rows)
+    // and one scatter row per warp
+    L.idx = o;
+    o += al16(2 * (size_t)T.sp.off_ba) + al16(2 * (size_t)T.sp.nnz_b) + al16(4 * (size_t)(T.sp.a + 1)) +
+         al16(4 * (size_t)T.sp.a) + al16(4 * (size_t)(T.sp.m + 1)) + al16(4 * (size_t)T.sp.N) + al16(4 * (size_t)T.sp.a);
+    L.wv = o; o += al16(mt * (size_t)MAXW * T.sp.N);
+  } else {
+    if (mat_smem) o += al16(mt * (size_t)(n + 2) * ld);
+    L.dinv = L.yv = L.rfs = L.idx = L.wv = o;
+  }
   L.total = o;
   return L;
 }
@@ -132,12 +151,26 @@ __device__ __forceinline__ unsigned long long mag_key(double v, bool cand) {
   return cand ? (unsigned long long)__double_as_longlong(v) : 0ull;
 }
 
-template <bool MIXED>
-struct CtaCell : Core<CtaCell<MIXED>, false, MIXED> {
+// SP (mixed only): the sparse bordered Newton matrix; the dense routines
+// (lu, invert_diagonal_blocks, lin_solve) then act on its trailing block
+template <bool MIXED, bool SP = false>
+struct CtaCell : Core<CtaCell<MIXED, SP>, false, MIXED> {
   using MT = typename std::conditional<MIXED, float, double>::type;
+  static_assert(!SP || MIXED, "the sparse Newton matrix is the mixed form's");
   const CtaArgs &A;
   const int tid, lane, warp, nw, n, ld;
   const bool owns;
+  // the dense matrix the dense routines factorise: order dn, stride dld
+  int dn, dld;
+  MT *dmat;
+  MT *S = nullptr;       // sparse: the matrix storage (leaf rows, trailing rows' leaf part, dense block)
+  MT *dinv = nullptr;    // sparse: reciprocal pivots of the leaf rows
+  MT *yv = nullptr;      // sparse: the solve's vector in elimination order
+  float *rfs = nullptr;  // sparse: row factor of each species row at assembly
+  // sparse: the index tables, copied to shared memory at the start
+  const unsigned short *sa_col = nullptr, *sb_col = nullptr;
+  const int *sa_ptr = nullptr, *sa_diag = nullptr, *sb_ptr = nullptr, *siperm = nullptr, *sul_rows = nullptr;
+  MT *wv = nullptr;      // sparse: [MAXW][N] one scatter row per warp
   const double inv_n;
   double *kn;            // global, this block's slot
   double *scr, *xs, *part;
@@ -156,11 +189,11 @@ struct CtaCell : Core<CtaCell<MIXED>, false, MIXED> {
 
   __device__ __forceinline__ CtaCell(const CtaArgs &a, int t)
       : A(a), tid(t), lane(t & 31), warp(t >> 5), nw(blockDim.x >> 5), n(a.n), ld(a.ld), owns(t < a.n),
-        inv_n(1.0 / a.n) {}
+        dn(a.n), dld(a.ld), dmat(nullptr), inv_n(1.0 / a.n) {}
 
   __device__ __forceinline__ bool leader() const { return tid == 0; }
   __device__ __forceinline__ void sync() const { __syncthreads(); }
-  __device__ __forceinline__ MT &M(int i, int j) const { return mat[(size_t)j * ld + i]; }
+  __device__ __forceinline__ MT &M(int i, int j) const { return dmat[(size_t)j * dld + i]; }
 
   // block-wide sums and maxima in a fixed order (every thread gets the value)
   __device__ __forceinline__ double sum_all(double v) {
@@ -390,9 +423,9 @@ struct CtaCell : Core<CtaCell<MIXED>, false, MIXED> {
 
   // LU with partial pivoting in place; false if a column has no nonzero pivot
   __device__ __forceinline__ bool lu() {
-    mystep = owns ? -1 : n;
-    for (int k0 = 0; k0 < n; k0 += PB) {
-      const int kb = min(PB, n - k0);
+    mystep = (tid < dn) ? -1 : dn;
+    for (int k0 = 0; k0 < dn; k0 += PB) {
+      const int kb = min(PB, dn - k0);
       for (int t = 0; t < kb; t++) {
         const int k = k0 + t;
         const bool cand = (mystep < 0);
@@ -412,7 +445,7 @@ struct CtaCell : Core<CtaCell<MIXED>, false, MIXED> {
       // whose U entries are all zero are left out of the trailing update
       const int j = k0 + kb + tid;
       bool nzc = false;
-      if (j < n) {
+      if (j < dn) {
         MT u[PB];
 #pragma unroll
         for (int t = 0; t < PB; t++) {
@@ -489,9 +522,9 @@ struct CtaCell : Core<CtaCell<MIXED>, false, MIXED> {
 
   // invert the 32x32 diagonal blocks of L (unit lower) and U in place
   __device__ __forceinline__ void invert_diagonal_blocks() {
-    const int nb = (n + DB - 1) / DB;
+    const int nb = (dn + DB - 1) / DB;
     for (int c = warp; c < nb; c += nw) {
-      const int k0 = c * DB, bs = min(DB, n - k0);
+      const int k0 = c * DB, bs = min(DB, dn - k0);
       const int t = lane;  // column of the block
       MT x[DB];
       // L^-1 column t: x_t = 1, x_r = -sum_{m=t}^{r-1} L_rm x_m
@@ -537,18 +570,232 @@ struct CtaCell : Core<CtaCell<MIXED>, false, MIXED> {
   }
 
   __device__ __forceinline__ bool setup(double yv) {
-    assemble(yv, -this->gamma);
-    bool ok = lu();
+    bool ok;
+    if constexpr (SP) {
+      assemble_sparse(yv, -this->gamma);
+      ok = sparse_lu();
+    } else {
+      assemble(yv, -this->gamma);
+      ok = lu();
+    }
     if (ok) {
       // any non-finite factor entry fails the setup (as a singular matrix)
       bool finite = true;
-      if (owns)
+      if constexpr (SP) {
+        for (int e = tid; e < A.tab.sp.total; e += blockDim.x) finite &= isfinite(S[e]);
+      } else if (owns) {
         for (int j = 0; j < n; j++) finite &= isfinite(M(tid, j));
+      }
       ok = __syncthreads_and(finite);
     }
     if (ok) invert_diagonal_blocks();
     this->after_setup();
     return ok;
+  }
+
+  // ---- the sparse bordered Newton matrix (mixed form) ----
+  //
+  // Unknowns: the species and x_e, in the plan's elimination order.  Rows:
+  // species i, W (I - gamma J) W^-1 with J taken at fixed x_e (its x_e column
+  // is df_i/dx_e); the x_e row, x_e - c^T x = 0 scaled the same way.  The
+  // correction of the species is the chain-rule system's.
+
+  // the matrix at y, times rf = -gamma, plus the identity, in the storage
+  __device__ __forceinline__ void assemble_sparse(double yv, double rf_d) {
+    const WarpTables &T = A.tab;
+    const auto &Q = T.sp;
+    const int G = T.lanes;
+    if (owns) xs[tid] = yv;
+    const float y32 = (float)yv;
+    ssc32 = fmaf(this->rtol32, fabsf(y32), this->atol32);
+    wsc32 = __frcp_rn(ssc32);
+    const float inv_atol = __frcp_rn(this->atol32);
+    if (owns) {
+      sig[tid] = ssc32 * inv_atol;
+      xs32[tid] = y32;
+      rfs[tid] = (float)rf_d * (wsc32 * this->atol32);   // -gamma / sig_i
+    }
+    const double xe = sum_all(owns ? cx * yv : 0.0);
+    const float xe32 = (float)xe;
+    // the x_e column's scale, from x_e like the species' (every thread has it)
+    const float sig_e = fmaf(this->rtol32, fabsf(xe32), this->atol32) * inv_atol;
+    MT *Da = reinterpret_cast<MT *>(scr);
+    MT *Db = Da + T.nreac;
+#pragma unroll 4
+    for (int r = tid; r < T.nreac; r += G) {
+      const int2 ab = __ldg(&T.rab[r]);
+      const float k32 = (float)kn[r];
+      const float sa = (ab.x == n) ? sig_e : sig[ab.x];
+      const float sb = (ab.y == n) ? sig_e : sig[ab.y];
+      Da[r] = k32 * ((ab.y == n ? xe32 : xs32[ab.y]) * sa);
+      Db[r] = k32 * ((ab.x == n ? xe32 : xs32[ab.x]) * sb);
+    }
+    for (int e = tid; e < Q.total; e += G) S[e] = MT(0);
+    __syncthreads();
+    {
+      MT *slots = upan;
+      MT s = MT(0);
+#pragma unroll 4
+      for (int t = 0; t < T.hlen; t++) {
+        const int x = __ldg(&T.h_x[t * G + tid]);
+        const int y = __ldg(&T.h_y[t * G + tid]);
+        const MT nu = __ldg(&T.h_nu_f[t * G + tid]);
+        const int r = x & 0xffff;
+        s = fma(nu, (x & 0x10000) ? Db[r] : Da[r], s);
+        const int kind = (x >> 17) & 3;
+        if (kind == 1) {
+          S[(unsigned)y >> 16] = s * rfs[y & 0xff];
+          s = MT(0);
+        } else if (kind == 2) {
+          slots[(unsigned)y >> 16] = s;
+          s = MT(0);
+        }
+      }
+      __syncthreads();
+      for (int b = tid; b < T.nbnd; b += G) {
+        const int tt = __ldg(&T.bnd_t[b]), ss = __ldg(&T.bnd_s[b]);
+        MT acc = MT(0);
+        for (int q = ss & 0xffff; q < (ss >> 16); q++) acc += slots[q];
+        S[(unsigned)tt >> 16] = acc * rfs[tt & 0xff];
+      }
+      __syncthreads();
+    }
+    // the identity, and the x_e row: -c_j sig_j / sig_e
+    for (int i = tid; i < Q.N; i += G) S[__ldg(&Q.diag_loc[i])] += MT(1);
+    if (owns) {
+      const int l = __ldg(&Q.e_loc[tid]);
+      if (l >= 0) S[l] = (MT)(-cx) * (sig[tid] * __frcp_rn(sig_e));
+    }
+    __syncthreads();
+  }
+
+  // in place: the leaf rows by dependency level, then the trailing rows'
+  // leaf-column part with its update of the dense block (no pivoting; one
+  // warp per row, the row scattered into the warp's dense row so that every
+  // update finds its entry by column), then the dense block with partial
+  // pivoting.  A row's eliminations run in column order; the updates of one
+  // elimination step go to distinct columns, one per lane.
+  __device__ __forceinline__ bool sparse_lu() {
+    const auto &Q = A.tab.sp;
+    const int a = Q.a;
+    MT *w = wv + (size_t)warp * Q.N;
+    bool ok = true;
+    for (int l = 0; l < Q.nlev; l++) {
+      const int r1 = __ldg(&Q.lev_ptr[l + 1]);
+      for (int r = __ldg(&Q.lev_ptr[l]) + warp; r < r1; r += nw) {
+        const int p0 = sa_ptr[r], pd = sa_diag[r], p1 = sa_ptr[r + 1];
+        for (int p = p0 + lane; p < p1; p += 32) w[sa_col[p]] = S[p];
+        __syncwarp();
+        for (int p = p0; p < pd; p++) {
+          const int k = sa_col[p];
+          const MT lk = w[k] * dinv[k];
+          const int u1 = sa_ptr[k + 1];
+          for (int u = sa_diag[k] + 1 + lane; u < u1; u += 32) {
+            const int j = sa_col[u];
+            w[j] = fma(-lk, S[u], w[j]);
+          }
+          if (lane == 0) S[p] = lk;
+          __syncwarp();
+        }
+        for (int p = pd + lane; p < p1; p += 32) S[p] = w[sa_col[p]];
+        if (lane == 0) {
+          const MT d = w[r];
+          ok &= (d != MT(0));
+          dinv[r] = rcp(d);
+        }
+        __syncwarp();
+      }
+      __syncthreads();
+    }
+    const int off_ba = Q.off_ba;
+    MT *D = S + Q.off_d;
+    for (int t = warp; t < Q.m; t += nw) {
+      const int p0 = sb_ptr[t], p1 = sb_ptr[t + 1];
+      for (int p = p0 + lane; p < p1; p += 32) w[sb_col[p]] = S[off_ba + p];
+      __syncwarp();
+      for (int p = p0; p < p1; p++) {
+        const int k = sb_col[p];
+        const MT lk = w[k] * dinv[k];
+        const int u1 = sa_ptr[k + 1];
+        for (int u = sa_diag[k] + 1 + lane; u < u1; u += 32) {
+          const int j = sa_col[u];
+          MT &dst = (j < a) ? w[j] : D[(size_t)(j - a) * Q.ldb + t];
+          dst = fma(-lk, S[u], dst);
+        }
+        if (lane == 0) S[off_ba + p] = lk;
+        __syncwarp();
+      }
+    }
+    if (!__syncthreads_and(ok)) return false;
+    return lu();
+  }
+
+  // x = M^-1 v (v this thread's species entry, scaled), the species part
+  __device__ __forceinline__ MT sparse_solve(MT v) {
+    const auto &Q = A.tab.sp;
+    const int a = Q.a;
+    if (owns) yv[siperm[tid]] = v;
+    if (tid == 0) yv[siperm[n]] = MT(0);
+    __syncthreads();
+    // forward, leaf rows
+    for (int l = 0; l < Q.nlev; l++) {
+      const int r1 = __ldg(&Q.lev_ptr[l + 1]);
+      for (int r = __ldg(&Q.lev_ptr[l]) + tid; r < r1; r += blockDim.x) {
+        MT s = yv[r];
+        const int pd = sa_diag[r];
+        for (int p = sa_ptr[r]; p < pd; p++) s = fma(-S[p], yv[sa_col[p]], s);
+        yv[r] = s;
+      }
+      __syncthreads();
+    }
+    // the trailing rows' leaf part, then the dense block
+    MT bt = MT(0);
+    if (tid < Q.m) {
+      MT s = yv[a + tid];
+      const int p1 = sb_ptr[tid + 1];
+      for (int p = sb_ptr[tid]; p < p1; p++) s = fma(-S[Q.off_ba + p], yv[sb_col[p]], s);
+      bt = s;
+    }
+    const MT xt = lin_solve(bt);
+    if (tid < Q.m) yv[a + tid] = xt;
+    __syncthreads();
+    // backward, leaf rows by U-dependency level
+    for (int l = 0; l < Q.nul; l++) {
+      const int i1 = __ldg(&Q.ul_ptr[l + 1]);
+      for (int i = __ldg(&Q.ul_ptr[l]) + tid; i < i1; i += blockDim.x) {
+        const int r = sul_rows[i];
+        MT s = yv[r];
+        const int pd = sa_diag[r], p1 = sa_ptr[r + 1];
+        for (int p = pd + 1; p < p1; p++) s = fma(-S[p], yv[sa_col[p]], s);
+        yv[r] = s * dinv[r];
+      }
+      __syncthreads();
+    }
+    const MT x = owns ? yv[siperm[tid]] : MT(0);
+    __syncthreads();
+    return x;
+  }
+
+  // copy the sparse index tables to shared memory (once per block)
+  __device__ __forceinline__ void stage_sparse(unsigned char *base) {
+    const auto &Q = A.tab.sp;
+    unsigned char *o = base;
+    auto take = [&](size_t bytes) { unsigned char *p = o; o += al16(bytes); return p; };
+    unsigned short *ac = reinterpret_cast<unsigned short *>(take(2 * (size_t)Q.off_ba));
+    unsigned short *bc = reinterpret_cast<unsigned short *>(take(2 * (size_t)Q.nnz_b));
+    int *ap = reinterpret_cast<int *>(take(4 * (size_t)(Q.a + 1)));
+    int *ad = reinterpret_cast<int *>(take(4 * (size_t)Q.a));
+    int *bp = reinterpret_cast<int *>(take(4 * (size_t)(Q.m + 1)));
+    int *ip = reinterpret_cast<int *>(take(4 * (size_t)Q.N));
+    int *ur = reinterpret_cast<int *>(take(4 * (size_t)Q.a));
+    for (int i = tid; i < Q.off_ba; i += blockDim.x) ac[i] = __ldg(&Q.a_col[i]);
+    for (int i = tid; i < Q.nnz_b; i += blockDim.x) bc[i] = __ldg(&Q.b_col[i]);
+    for (int i = tid; i <= Q.a; i += blockDim.x) ap[i] = __ldg(&Q.a_ptr[i]);
+    for (int i = tid; i < Q.a; i += blockDim.x) { ad[i] = __ldg(&Q.a_diag[i]); ur[i] = __ldg(&Q.ul_rows[i]); }
+    for (int i = tid; i <= Q.m; i += blockDim.x) bp[i] = __ldg(&Q.b_ptr[i]);
+    for (int i = tid; i < Q.N; i += blockDim.x) ip[i] = __ldg(&Q.iperm[i]);
+    sa_col = ac; sb_col = bc; sa_ptr = ap; sa_diag = ad; sb_ptr = bp; siperm = ip; sul_rows = ur;
+    __syncthreads();
   }
 
   // x = M^-1 b for this thread's component (FP64 form)
@@ -561,7 +808,9 @@ struct CtaCell : Core<CtaCell<MIXED>, false, MIXED> {
   // of the FP32 matrix); the correction comes back times ssc*gscale, in FP32
   // for the norm and in FP64 for the state
   __device__ __forceinline__ double solve32(double b, float gs, float &x32) {
-    const MT xv = lin_solve(owns ? (float)b * wsc32 : 0.0f);
+    MT xv;
+    if constexpr (SP) xv = sparse_solve(owns ? (float)b * wsc32 : 0.0f);
+    else xv = lin_solve(owns ? (float)b * wsc32 : 0.0f);
     x32 = owns ? xv * (ssc32 * gs) : 0.0f;
     return (double)x32;
   }
@@ -569,12 +818,13 @@ struct CtaCell : Core<CtaCell<MIXED>, false, MIXED> {
   // the triangular solves with the factors in place: v is this thread's
   // right-hand-side entry, the solution component of its species is returned
   __device__ __forceinline__ MT lin_solve(MT v) {
-    const int nb = (n + DB - 1) / DB;
+    const int nb = (dn + DB - 1) / DB;
+    const bool downs = tid < dn;
     bsv[tid] = v;
     __syncthreads();
     // forward: L y = P b
     for (int c = 0; c < nb; c++) {
-      const int k0 = c * DB, bs = min(DB, n - k0);
+      const int k0 = c * DB, bs = min(DB, dn - k0);
       if (warp == c % nw) {
         const int pr = (lane < bs) ? perm[k0 + lane] : 0;
         const MT s = (lane < bs) ? bsv[pr] : MT(0);
@@ -587,7 +837,7 @@ struct CtaCell : Core<CtaCell<MIXED>, false, MIXED> {
         if (lane < bs) ys[k0 + lane] = y;
       }
       __syncthreads();
-      if (mystep >= k0 + bs && owns) {
+      if (mystep >= k0 + bs && downs) {
         MT s = v;
         for (int t = 0; t < bs; t++) s = fma(-M(tid, k0 + t), ys[k0 + t], s);
         v = s;
@@ -596,11 +846,11 @@ struct CtaCell : Core<CtaCell<MIXED>, false, MIXED> {
       __syncthreads();
     }
     // backward: U x = y; the running value of logical row k is kept by its pivot row
-    v = owns ? ys[mystep] : MT(0);
+    v = downs ? ys[mystep] : MT(0);
     bsv[tid] = v;
     __syncthreads();
     for (int c = nb - 1; c >= 0; c--) {
-      const int k0 = c * DB, bs = min(DB, n - k0);
+      const int k0 = c * DB, bs = min(DB, dn - k0);
       if (warp == c % nw) {
         // x_r = sum_{t>=r} Uinv_rt s_t, s_t the running value of logical row k0+t
         const int pr = (lane < bs) ? perm[k0 + lane] : 0;
@@ -614,7 +864,7 @@ struct CtaCell : Core<CtaCell<MIXED>, false, MIXED> {
         if (lane < bs) ys[k0 + lane] = x;
       }
       __syncthreads();
-      if (owns && mystep < k0) {
+      if (downs && mystep < k0) {
         MT s = v;
         for (int t = 0; t < bs; t++) s = fma(-M(tid, k0 + t), ys[k0 + t], s);
         v = s;
@@ -622,8 +872,8 @@ struct CtaCell : Core<CtaCell<MIXED>, false, MIXED> {
       }
       __syncthreads();
     }
-    // ys[k] is now the solution component of column k = species k
-    const MT xv = owns ? ys[tid] : MT(0);
+    // ys[k] is now the solution component of column k
+    const MT xv = downs ? ys[tid] : MT(0);
     __syncthreads();
     return xv;
   }
@@ -675,13 +925,13 @@ struct CtaCell : Core<CtaCell<MIXED>, false, MIXED> {
   }
 };
 
-template <bool MIXED>
-__global__ void __launch_bounds__(256, 1) chem_cta_kernel(const __grid_constant__ CtaArgs A, int total_cells,
+template <bool MIXED, bool SP>
+__global__ void __launch_bounds__(256, SP ? 2 : 1) chem_cta_kernel(const __grid_constant__ CtaArgs A, int total_cells,
                                                           const int *total_ptr, int mat_smem) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   using MT = typename std::conditional<MIXED, float, double>::type;
-  const CtaLayout L = cta_layout(A.tab, A.ld, sizeof(MT), mat_smem != 0);
-  CtaCell<MIXED> c(A, threadIdx.x);
+  const CtaLayout L = cta_layout(A.tab, A.ld, sizeof(MT), mat_smem != 0, SP);
+  CtaCell<MIXED, SP> c(A, threadIdx.x);
   c.kn = A.kn_global + (size_t)blockIdx.x * (A.tab.nkn + 1);
   c.scr = reinterpret_cast<double *>(smem_raw + L.scr);
   c.xs = reinterpret_cast<double *>(smem_raw + L.xs);
@@ -701,6 +951,18 @@ __global__ void __launch_bounds__(256, 1) chem_cta_kernel(const __grid_constant_
   c.wu = reinterpret_cast<CoefUniform *>(smem_raw + L.wu);
   c.mat = mat_smem ? reinterpret_cast<MT *>(smem_raw + L.mat)
                    : reinterpret_cast<MT *>(A.mat_global) + (size_t)blockIdx.x * (A.n + 2) * A.ld;
+  c.dmat = c.mat;
+  if constexpr (SP) {
+    c.S = reinterpret_cast<MT *>(smem_raw + L.mat);
+    c.dinv = reinterpret_cast<MT *>(smem_raw + L.dinv);
+    c.yv = reinterpret_cast<MT *>(smem_raw + L.yv);
+    c.rfs = reinterpret_cast<float *>(smem_raw + L.rfs);
+    c.dmat = c.S + A.tab.sp.off_d;
+    c.dn = A.tab.sp.m;
+    c.dld = A.tab.sp.ldb;
+    c.wv = reinterpret_cast<MT *>(smem_raw + L.wv);
+    c.stage_sparse(smem_raw + L.idx);
+  }
   c.build_uniform_table();
   if (total_ptr) total_cells = *total_ptr;
   __shared__ int next_idx;
@@ -759,6 +1021,7 @@ __global__ void __launch_bounds__(256, 1) eval_cta_kernel(const __grid_constant_
   c.wu = reinterpret_cast<CoefUniform *>(smem_raw + L.wu);
   c.mat = mat_smem ? reinterpret_cast<double *>(smem_raw + L.mat)
                    : reinterpret_cast<double *>(A.mat_global) + (size_t)blockIdx.x * (n + 2) * A.ld;
+  c.dmat = c.mat;
   c.rtol = A.reltol;
   c.atol = A.abstol;
   c.cx = (tid < n) ? __ldg(&A.tab.xe_coef[tid]) : 0.0;
@@ -787,19 +1050,43 @@ __global__ void __launch_bounds__(256, 1) eval_cta_kernel(const __grid_constant_
 
 }  // namespace
 
+#ifndef PDR_CTA_SPARSE
+#define PDR_CTA_SPARSE 1
+#endif
+
+static int optin_smem() {
+  int dev = 0, optin = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  return optin;
+}
+
+// the mixed form runs on the sparse Newton matrix when the network has its
+// plan and the block's arrays fit shared memory
+static bool cta_sparse(const pdr_net *net, bool mixed) {
+  const WarpTables &T = net->cta;
+  if (!PDR_CTA_SPARSE || !mixed || !T.sp.ok) return false;
+  return cta_layout(T, T.neq | 1, 4, true, true).total + 64 <= (size_t)optin_smem();
+}
+
 // shared memory of one block, and whether the matrix is in it
 size_t chem_cta_smem(const pdr_net *net, bool mixed, bool *mat_smem) {
   const WarpTables &T = net->cta;
   const int n = T.neq, ld = n | 1;
   const size_t mt = mixed ? 4 : 8;
+  if (cta_sparse(net, mixed)) { *mat_smem = true; return cta_layout(T, ld, 4, true, true).total; }
   CtaLayout with = cta_layout(T, ld, mt, true);
-  int dev = 0, optin = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  if (with.total + 64 <= (size_t)optin) { *mat_smem = true; return with.total; }   // + static shared
+  if (with.total + 64 <= (size_t)optin_smem()) { *mat_smem = true; return with.total; }   // + static shared
   *mat_smem = false;
   return cta_layout(T, ld, mt, false).total;
 }
+
+using CtaKernel = void (*)(const CtaArgs, int, const int *, int);
+static CtaKernel cta_kernel(int variant) {
+  return variant == 0 ? chem_cta_kernel<false, false> : (variant == 1 ? chem_cta_kernel<true, false>
+                                                                       : chem_cta_kernel<true, true>);
+}
+static int cta_variant(const pdr_net *net, bool mixed) { return !mixed ? 0 : (cta_sparse(net, mixed) ? 2 : 1); }
 
 // Per-launch global scratch of the block integrator: rate constants and, when
 // the matrix does not fit shared memory, the matrix, one slot per block.
@@ -816,18 +1103,17 @@ size_t chem_cta_global_bytes(const pdr_net *net, bool mixed, int grid) {
 // The dynamic shared-memory limit of a kernel is set per device and only ever
 // grows there (networks of different sizes share the two kernels), so no call
 // lowers it below what another network's launch needs.
-static cudaError_t ensure_smem_attr(bool mixed, size_t smem) {
+static cudaError_t ensure_smem_attr(int variant, size_t smem) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   dev &= 63;
   static std::mutex mu;
-  static size_t attr[64][2] = {};
+  static size_t attr[64][3] = {};
   std::lock_guard<std::mutex> lk(mu);
-  if (smem <= attr[dev][mixed]) return cudaSuccess;
-  auto k = mixed ? chem_cta_kernel<true> : chem_cta_kernel<false>;
-  e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e == cudaSuccess) attr[dev][mixed] = smem;
+  if (smem <= attr[dev][variant]) return cudaSuccess;
+  e = cudaFuncSetAttribute(cta_kernel(variant), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess) attr[dev][variant] = smem;
   return e;
 }
 
@@ -835,8 +1121,9 @@ static cudaError_t ensure_smem_attr(bool mixed, size_t smem) {
 int chem_cta_blocks_per_sm(const pdr_net *net, bool mixed) {
   bool ms = false;
   const size_t smem = chem_cta_smem(net, mixed, &ms);
-  auto k = mixed ? chem_cta_kernel<true> : chem_cta_kernel<false>;
-  if (ensure_smem_attr(mixed, smem) != cudaSuccess) return 0;
+  const int variant = cta_variant(net, mixed);
+  auto k = cta_kernel(variant);
+  if (ensure_smem_attr(variant, smem) != cudaSuccess) return 0;
   int per_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, net->cta.lanes, smem) != cudaSuccess) return 0;
   return per_sm;
@@ -881,8 +1168,9 @@ int launch_chem_cta(const pdr_net *net, int ncell, double *ab, const double *rat
   const size_t smem = chem_cta_smem(net, mixed, &ms);
   A.kn_global = reinterpret_cast<double *>(scratch);
   A.mat_global = ms ? nullptr : reinterpret_cast<unsigned char *>(scratch) + al16((size_t)grid * (T.nkn + 1) * 8);
-  auto k = mixed ? chem_cta_kernel<true> : chem_cta_kernel<false>;
-  cudaError_t ea = ensure_smem_attr(mixed, smem);
+  const int variant = cta_variant(net, mixed);
+  auto k = cta_kernel(variant);
+  cudaError_t ea = ensure_smem_attr(variant, smem);
   if (ea != cudaSuccess) return cuda_fail(ea, "cudaFuncSetAttribute(chem_cta_kernel)");
   k<<<grid, T.lanes, smem, st>>>(A, ncell, total_ptr, ms ? 1 : 0);
   cudaError_t e = cudaGetLastError();

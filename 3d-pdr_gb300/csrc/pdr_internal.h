@@ -66,8 +66,38 @@ struct WarpTables {
   int *h_y = nullptr;         // [hlen][lanes] row | column << 8 | slot << 16
   double *h_nu = nullptr;     // [hlen][lanes] nu (0 = padding)
   float *h_nu_f = nullptr;
-  int *bnd_t = nullptr;       // [nbnd] row | column << 8 of a boundary entry
+  int *bnd_t = nullptr;       // [nbnd] row | column << 8 | sparse location << 16 of a boundary entry
   int *bnd_s = nullptr;       // [nbnd] first slot | (last slot + 1) << 16
+  // Sparse Newton matrix of the block integrator's mixed form (sp.ok): the
+  // bordered system over the N = neq+1 unknowns (species, then x_e with the
+  // row x_e - sum_j c_j x_j = 0) instead of the x_e chain rule, whose rank-one
+  // term fills most of the matrix.  Unknowns in a minimum-degree elimination
+  // order; the first `a` rows (the "leaf" rows: few dependencies) stored
+  // packed by row and factorised in place without pivoting, one dependency
+  // level at a time; the last m = N - a rows, nearly dense after fill, hold
+  // their leaf-column part packed and their trailing m x m block dense
+  // (column-major, stride ldb), factorised with partial pivoting.  For a
+  // kind-1 term entry the high 16 bits of h_y hold its location in the
+  // storage, for a boundary entry those of bnd_t.
+  struct Sparse {
+    int ok = 0;
+    int N = 0, a = 0, m = 0, ldb = 0;
+    int off_ba = 0, off_d = 0, total = 0;   // storage offsets / size, in elements
+    int nnz_b = 0;                          // trailing rows' leaf-column entries
+    int nlev = 0, nul = 0;
+    int *perm = nullptr;      // [N] unknown (elimination order) -> slot (species, neq = x_e)
+    int *iperm = nullptr;     // [N] slot -> unknown
+    int *a_ptr = nullptr;     // [a+1] leaf row r: storage [a_ptr[r], a_ptr[r+1])
+    unsigned short *a_col = nullptr;   // column (unknown) of each leaf-row entry, ascending
+    int *a_diag = nullptr;    // [a] storage position of the diagonal
+    int *lev_ptr = nullptr;   // [nlev+1] leaf rows by L-dependency level (rows are in level order)
+    int *ul_rows = nullptr;   // [a] leaf rows by U-dependency level
+    int *ul_ptr = nullptr;    // [nul+1]
+    int *b_ptr = nullptr;     // [m+1] trailing row t: leaf-column entries at off_ba + [b_ptr[t], b_ptr[t+1])
+    unsigned short *b_col = nullptr;   // their columns, ascending
+    int *diag_loc = nullptr;  // [N] storage location of each diagonal entry
+    int *e_loc = nullptr;     // [neq] location of (x_e row, species j), -1 where c_j = 0
+  } sp;
 };
 
 // Device tables for the rate evaluator.

@@ -8,6 +8,7 @@
 // tables the kernels read: reactant slots per reaction, the net stoichiometry as
 // per-species term lists, and their balanced split over the 32 lanes of a warp.
 #include <algorithm>
+#include <bitset>
 #include <limits>
 #include <cmath>
 #include <cstdio>
@@ -203,6 +204,209 @@ static T *upload(pdr_net *net, const std::vector<T> &v, int &rc) {
   return d;
 }
 
+// ---- sparse Newton matrix of the block integrator (mixed form) ----
+//
+// The chain rule through x_e = sum_j c_j x_j adds (df/dx_e) c^T to the
+// Jacobian: a rank-one term that fills the rows of every species with an
+// electron reaction in the columns of every charged species (two thirds of
+// the full network's 214 x 214 entries).  Keeping x_e as an unknown of its
+// own, with the linearised constraint x_e - c^T x = 0 as an extra row, gives
+// the same Newton correction from a matrix with a seventh of the entries.
+// This plan orders the unknowns (minimum degree), computes the fill of the
+// factorisation in that order, splits the rows into packed "leaf" rows and a
+// dense trailing block, and maps every Jacobian entry to its storage location.
+struct SparsePlan {
+  int N = 0, a = 0, m = 0, ldb = 0, off_ba = 0, off_d = 0, total = 0;
+  std::vector<int> perm, iperm, a_ptr, a_diag, lev_ptr, ul_rows, ul_ptr, b_ptr, diag_loc, e_loc;
+  std::vector<unsigned short> a_col, b_col;
+  std::vector<std::bitset<256>> F;   // filled pattern in elimination order
+  // storage location of entry (unknown i, unknown j), -1 outside the pattern
+  int loc(int i, int j) const {
+    if (i < a) {
+      for (int p = a_ptr[i]; p < a_ptr[i + 1]; p++)
+        if (a_col[p] == j) return p;
+      return -1;
+    }
+    const int t = i - a;
+    if (j < a) {
+      for (int p = b_ptr[t]; p < b_ptr[t + 1]; p++)
+        if (b_col[p] == j) return off_ba + p;
+      return -1;
+    }
+    return off_d + (j - a) * ldb + t;
+  }
+};
+
+using Bits = std::bitset<256>;
+
+// symbolic LU fill without pivoting of pattern P (rows as bitsets)
+static std::vector<Bits> symbolic_fill(std::vector<Bits> F) {
+  const int N = (int)F.size();
+  for (int k = 0; k < N; k++) {
+    Bits right = F[k];
+    for (int j = 0; j <= k; j++) right.reset(j);
+    for (int i = k + 1; i < N; i++)
+      if (F[i].test(k)) F[i] |= right;
+  }
+  return F;
+}
+
+// pattern entries (row, column) over slots (species 0..neq-1, x_e = neq);
+// G threads per block (for the cost model)
+static bool sparse_plan(int neq, const std::vector<std::pair<int, int>> &entries, const std::vector<int> &xe,
+                        int G, SparsePlan &sp) {
+  const int N = neq + 1;
+  if (N > 256) return false;
+  std::vector<Bits> P(N);
+  for (int i = 0; i < N; i++) P[i].set(i);
+  for (auto &e : entries) P[e.first].set(e.second);
+  for (int j = 0; j < neq; j++)
+    if (xe[j] != 0) P[neq].set(j);
+  // minimum-degree order on the symmetrised pattern (ties: lowest slot)
+  std::vector<int> order;
+  {
+    std::vector<Bits> adj(N);
+    for (int i = 0; i < N; i++)
+      for (int j = 0; j < N; j++)
+        if (i != j && (P[i].test(j) || P[j].test(i))) adj[i].set(j);
+    Bits alive;
+    for (int i = 0; i < N; i++) alive.set(i);
+    for (int step = 0; step < N; step++) {
+      int best = -1;
+      size_t bd = 0;
+      for (int v = 0; v < N; v++) {
+        if (!alive.test(v)) continue;
+        const size_t d = (adj[v] & alive).count();
+        if (best < 0 || d < bd) { best = v; bd = d; }
+      }
+      order.push_back(best);
+      alive.reset(best);
+      const Bits nb = adj[best] & alive;
+      for (int u = 0; u < N; u++)
+        if (nb.test(u)) { adj[u] |= nb; adj[u].reset(u); }
+    }
+  }
+  auto permuted = [&](const std::vector<int> &ord) {
+    std::vector<Bits> Q(N);
+    for (int i = 0; i < N; i++)
+      for (int j = 0; j < N; j++)
+        if (P[ord[i]].test(ord[j])) Q[i].set(j);
+    return symbolic_fill(Q);
+  };
+  std::vector<Bits> F = permuted(order);
+  // L-dependency level of each row: 1 + the deepest row it reads
+  std::vector<int> lev(N, 1);
+  int maxlev = 0;
+  for (int i = 0; i < N; i++) {
+    for (int k = 0; k < i; k++)
+      if (F[i].test(k)) lev[i] = std::max(lev[i], lev[k] + 1);
+    maxlev = std::max(maxlev, lev[i]);
+  }
+  // split: the rows of levels <= s are leaf rows.  Cost model per
+  // factorisation: the dense block's FMAs spread over G threads, a block
+  // barrier per dense column and per leaf level, and the longest leaf row
+  // (one thread each) of every level
+  std::vector<int> ucount(N, 0);
+  for (int k = 0; k < N; k++)
+    for (int j = k + 1; j < N; j++) ucount[k] += F[k].test(j);
+  int best_s = 0;
+  double best_cost = 0.0;
+  for (int s = 0; s <= maxlev; s++) {
+    int a = 0;
+    double rowwork = 0.0;
+    std::vector<double> lw(s + 1, 0.0);
+    for (int i = 0; i < N; i++)
+      if (lev[i] <= s) {
+        a++;
+        double w = 0.0;
+        for (int k = 0; k < i; k++)
+          if (F[i].test(k)) w += 1 + ucount[k];
+        lw[lev[i]] = std::max(lw[lev[i]], w);
+      }
+    for (double w : lw) rowwork += w;
+    const double m = N - a;
+    const double cost = 4.0 * (2.0 / 3.0) * m * m * m / G + 250.0 * (m + s) + 12.0 * rowwork;
+    if (s == 0 || cost < best_cost) { best_cost = cost; best_s = s; }
+  }
+  // final order: leaf rows by level (rows of one level are independent, so
+  // this keeps the fill), then the trailing rows in minimum-degree order
+  std::vector<int> idx;
+  for (int l = 1; l <= best_s; l++)
+    for (int i = 0; i < N; i++)
+      if (lev[i] == l) idx.push_back(i);
+  const int a = (int)idx.size();
+  for (int i = 0; i < N; i++)
+    if (lev[i] > best_s) idx.push_back(i);
+  std::vector<int> ord2(N);
+  for (int i = 0; i < N; i++) ord2[i] = order[idx[i]];
+  F = permuted(ord2);
+  const int m = N - a;
+  for (int i = a; i < N; i++)
+    for (int j = a; j < N; j++) F[i].set(j);   // the trailing block is stored dense
+  sp.N = N;
+  sp.a = a;
+  sp.m = m;
+  sp.ldb = m | 1;
+  sp.perm = ord2;
+  sp.iperm.assign(N, 0);
+  for (int i = 0; i < N; i++) sp.iperm[ord2[i]] = i;
+  // leaf rows, packed; their levels
+  sp.a_ptr.assign(1, 0);
+  sp.lev_ptr.assign(1, 0);
+  std::vector<int> lev2(N, 1);
+  for (int i = 0; i < a; i++) {
+    for (int k = 0; k < i; k++)
+      if (F[i].test(k)) lev2[i] = std::max(lev2[i], lev2[k] + 1);
+    for (int j = 0; j < N; j++)
+      if (F[i].test(j)) {
+        if (j == i) sp.a_diag.push_back((int)sp.a_col.size());
+        sp.a_col.push_back((unsigned short)j);
+      }
+    sp.a_ptr.push_back((int)sp.a_col.size());
+  }
+  for (int i = 0; i < a; i++) {
+    if (i > 0 && lev2[i] < lev2[i - 1]) return false;   // rows must be in level order
+    if (i == 0 || lev2[i] != lev2[i - 1]) {
+      if (i > 0) sp.lev_ptr.push_back(i);
+    }
+  }
+  if (a > 0) sp.lev_ptr.push_back(a);
+  // U-dependency levels of the leaf rows (backward substitution)
+  std::vector<int> ul(a, 1);
+  int maxul = 0;
+  for (int i = a - 1; i >= 0; i--) {
+    for (int j = i + 1; j < a; j++)
+      if (F[i].test(j)) ul[i] = std::max(ul[i], ul[j] + 1);
+    maxul = std::max(maxul, ul[i]);
+  }
+  sp.ul_ptr.assign(1, 0);
+  for (int l = 1; l <= maxul; l++) {
+    for (int i = 0; i < a; i++)
+      if (ul[i] == l) sp.ul_rows.push_back(i);
+    sp.ul_ptr.push_back((int)sp.ul_rows.size());
+  }
+  // trailing rows: leaf-column entries packed, then the dense block
+  sp.b_ptr.assign(1, 0);
+  for (int i = a; i < N; i++) {
+    for (int j = 0; j < a; j++)
+      if (F[i].test(j)) sp.b_col.push_back((unsigned short)j);
+    sp.b_ptr.push_back((int)sp.b_col.size());
+  }
+  sp.off_ba = (int)sp.a_col.size();
+  sp.off_d = (sp.off_ba + (int)sp.b_col.size() + 3) & ~3;
+  sp.total = sp.off_d + m * sp.ldb;
+  if (sp.total >= 65536) return false;
+  sp.F = F;
+  sp.diag_loc.assign(N, -1);
+  for (int i = 0; i < N; i++) sp.diag_loc[i] = sp.loc(i, i);
+  sp.e_loc.assign(neq, -1);
+  for (int j = 0; j < neq; j++)
+    if (xe[j] != 0) sp.e_loc[j] = sp.loc(sp.iperm[neq], sp.iperm[j]);
+  for (int v : sp.diag_loc)
+    if (v < 0) return false;
+  return true;
+}
+
 int build_device_tables(pdr_net *net) {
   const HostNet &h = net->host;
   int rc = 0;
@@ -382,6 +586,7 @@ int build_device_tables(pdr_net *net) {
     for (int i = 0; i < neq; i++) xe[i] = h.xe[i];
     // term-parallel Jacobian tables (both integrators)
     std::vector<int> hx, hy, bt, bs;
+    SparsePlan plan;
     std::vector<double> hn;
     std::vector<float> hnf;
     {
@@ -399,6 +604,18 @@ int build_device_tables(pdr_net *net) {
         return x.which < y.which;
       });
       const int H = (int)hs.size();
+      // the block integrator's sparse Newton matrix: entry locations
+      if (G > kWarp) {
+        std::vector<std::pair<int, int>> ent;
+        for (auto &x : hs) ent.push_back({x.i, x.col});
+        w.sp.ok = sparse_plan(neq, ent, h.xe, G, plan) ? 1 : 0;
+      }
+      auto sp_loc = [&](int i, int col) -> unsigned {
+        if (!w.sp.ok) return 0u;
+        const int l = plan.loc(plan.iperm[i], plan.iperm[col]);
+        if (l < 0) w.sp.ok = 0;
+        return l < 0 ? 0u : (unsigned)l;
+      };
       w.hlen = std::max(1, (H + G - 1) / G);
       hx.assign((size_t)w.hlen * G, 0);
       hy.assign((size_t)w.hlen * G, 0);
@@ -421,13 +638,15 @@ int build_device_tables(pdr_net *net) {
               if (kind == 2) sl = slot++;
             }
             hx[(size_t)t * G + c] = hs[k].r | (hs[k].which << 16) | (kind << 17);
-            hy[(size_t)t * G + c] = hs[k].i | (hs[k].col << 8) | (sl << 16);
+            // kind 1 (a store): the entry's sparse location; kind 2: its slot
+            const unsigned hi = (kind == 1) ? sp_loc(hs[k].i, hs[k].col) : (unsigned)sl;
+            hy[(size_t)t * G + c] = (int)((unsigned)hs[k].i | ((unsigned)hs[k].col << 8) | (hi << 16));
             hn[(size_t)t * G + c] = hs[k].nu;
             hnf[(size_t)t * G + c] = (float)hs[k].nu;
           }
         }
         if (c0 != c1) {
-          bt.push_back(hs[e0].i | (hs[e0].col << 8));
+          bt.push_back((int)((unsigned)hs[e0].i | ((unsigned)hs[e0].col << 8) | (sp_loc(hs[e0].i, hs[e0].col) << 16)));
           bs.push_back(first_slot | (slot << 16));
         }
         e0 = e1;
@@ -461,6 +680,26 @@ int build_device_tables(pdr_net *net) {
         w.bnd_t = upload(net, bt, rc2);
         w.bnd_s = upload(net, bs, rc2);
       }
+    }
+    if (w.sp.ok) {
+      auto &d = w.sp;
+      d.N = plan.N; d.a = plan.a; d.m = plan.m; d.ldb = plan.ldb;
+      d.off_ba = plan.off_ba; d.off_d = plan.off_d; d.total = plan.total;
+      d.nnz_b = (int)plan.b_col.size();
+      d.nlev = (int)plan.lev_ptr.size() - 1;
+      d.nul = (int)plan.ul_ptr.size() - 1;
+      d.perm = upload(net, plan.perm, rc2);
+      d.iperm = upload(net, plan.iperm, rc2);
+      d.a_ptr = upload(net, plan.a_ptr, rc2);
+      d.a_col = upload(net, plan.a_col, rc2);
+      d.a_diag = upload(net, plan.a_diag, rc2);
+      d.lev_ptr = upload(net, plan.lev_ptr, rc2);
+      d.ul_rows = upload(net, plan.ul_rows, rc2);
+      d.ul_ptr = upload(net, plan.ul_ptr, rc2);
+      d.b_ptr = upload(net, plan.b_ptr, rc2);
+      d.b_col = upload(net, plan.b_col, rc2);
+      d.diag_loc = upload(net, plan.diag_loc, rc2);
+      d.e_loc = upload(net, plan.e_loc, rc2);
     }
     return rc2;
   };

@@ -46,6 +46,7 @@ CONFIGS = {"C1": dict(network="reduced", ncell=64, seed=1001,
            "C2": dict(network="full", ncell=32768, seed=1002,
                       text="full network, 32^3 = 32768 cells (C2), t_end 1e7 yr, rtol 1e-8, atol 1e-30")}
 FALLBACK_HBM_GBS = 6800.0
+CASES = ["rates", "heating", "lte-CO", "levpop-CII", "levpop-CO", "columns", "tau", "thermal", "levconv"]
 
 
 def parse():
@@ -60,6 +61,8 @@ def parse():
     p.add_argument("--no-extras", action="store_true", help="headline only (profiling runs)")
     p.add_argument("--no-autotune", action="store_true", help="default launch shape (profiling runs)")
     p.add_argument("--no-secondary", action="store_true", help="skip the secondary configuration lines")
+    p.add_argument("--case", default="", choices=[""] + sorted(CASES),
+                   help="one kernel alone on a small case (profiling): a warm-up call, then --steps timed calls")
     return p.parse_args()
 
 
@@ -582,6 +585,81 @@ def thermal_controllers(G, W, dev, stream, n=1 << 23, n_lev=1 << 20):
                              "sample": f"first {1 << 18} cells, oracle thermal pass ({cdt * 1e3:.1f} ms)"}}
 
 
+def kernel_case(a):
+    """One kernel of the path alone (profiling captures): its inputs, one
+    warm-up call, then a.steps timed calls; prints the mean CUDA-event time.
+    --ncell sets the cell count (rays cases: the lattice side)."""
+    import torch
+    import pdrgpu as G
+    import workloads as W
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.Stream(device=dev)
+    name = a.case
+    d = lambda x: torch.as_tensor(np.ascontiguousarray(x), device=dev)
+    if name in ("rates", "heating"):
+        n = a.ncell or 262144
+        w = W.chemistry("C3", ncell=n, seed=CONFIGS["C3"]["seed"])
+        net = G.Network("reduced")
+        ph = G.phys(w.zeta, w.omega, w.grain_radius, w.metallicity, w.g2d, w.v_turb_kms)
+        args = [d(w.T), d(w.Td), d(w.rad_surface), d(w.AV), d(w.column5)]
+        rate, _ = G.reaction_rates(net, ph, *args, stream=stream)
+        if name == "rates":
+            fn = lambda: G.reaction_rates(net, ph, *args, rate=rate, stream=stream)
+        else:
+            ab = d(np.tile(W.initial_abundances(net.species), (n, 1)))
+            uv = d(w.G0)
+            dens = d(w.n_H)
+            fn = lambda: G.heating(net, 0, ph, dens, args[0], args[1], uv, ab, rate, stream=stream)
+    elif name.startswith("levpop-") or name.startswith("lte-"):
+        key = name.split("-")[1]
+        n = a.ncell or 65536
+        lp = W.levpop(ncell=n)
+        cool = G.Coolant(key)
+        nH, T, Td, p5 = (d(lp[k]) for k in ("n_H", "T", "Td", "partner5"))
+        dens = nH * W.COOLANT_X[key]
+        spop, _ = G.lte_populations(cool, T, dens, stream=stream)
+        tau = d(W.levpop_tau(n, cool.nlin, seed=lp["seed"] + 1))
+        if name.startswith("lte-"):
+            fn = lambda: G.lte_populations(cool, T, dens, stream=stream)
+        else:
+            prec = os.environ.get("PDR_LEVPOP_PRECISION", "fp64")
+            fn = lambda: G.level_populations(cool, nH, T, Td, p5, dens, spop, tau, precision=prec, stream=stream)
+    elif name in ("columns", "tau"):
+        side = a.ncell or 48
+        r = W.rays(side, 12, nspec=33, seed=1008)
+        rays, keep = G.device_rays(r, dev)
+        rho = d(r["rho"])
+        if name == "columns":
+            ab = d(r["abundance"])
+            fn = lambda: (G.uvfield(rays, rho, 0, (10.0, 0.0, 0.0), r["vectors"], stream=stream),
+                          G.column_densities(rays, rho, ab, [0, 5, 12, 20, 31], stream=stream))
+        else:
+            cool = G.Coolant("CO")
+            Tg = d(W._rng(1009).uniform(10.0, 300.0, r["ngrid"]))
+            pop, _ = G.lte_populations(cool, Tg, rho * W.COOLANT_X["CO"], stream=stream)
+            fn = lambda: G.optical_depths(cool, rays, pop, Tg, 1.0e5, stream=stream)
+    elif name == "thermal":
+        n = a.ncell or (1 << 23)
+        rng = W._rng(1010)
+        tb = G.ThermalBalance(d(rng.uniform(10.0, 3000.0, n)))
+        heat = d(10.0 ** rng.uniform(-24, -20, n))
+        cool = [heat * float(f) for f in (0.1, 0.2, 0.3, 0.4)]
+        fn = lambda: tb.update(heat, cool, 1, 1, stream=stream)
+    else:   # levconv
+        n = a.ncell or (1 << 20)
+        rng = W._rng(1010)
+        sols = [d(10.0 ** rng.uniform(-10, 0, (n, m))) for m in (5, 5, 5, 41)]
+        pops = [s * 1.001 for s in sols]
+        ab = d(10.0 ** rng.uniform(-8, -3, (n, 33)))
+        lc = G.ThermalBalance(torch.zeros(n, dtype=torch.float64, device=dev))
+        fn = lambda: lc.level_convergence(sols, pops, ab, (0, 5, 12, 20), stream=stream)
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        fn()
+        ms = _timed(fn, stream, max(1, a.steps))
+    print(json.dumps({"case": name, "ncell": a.ncell or None, "ms_per_call": ms, "calls_timed": max(1, a.steps)}))
+
+
 def run_reference(a, rank):
     if rank != 0:
         return
@@ -609,6 +687,8 @@ def run_reference(a, rank):
 
 def main():
     a = parse()
+    if a.case:
+        return kernel_case(a)
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if a.impl == "reference":
