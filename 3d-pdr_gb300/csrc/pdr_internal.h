@@ -109,6 +109,12 @@ struct RateTables {
   double *alpha = nullptr, *beta = nullptr, *gamma = nullptr, *rtmin = nullptr, *rtmax = nullptr;
   int *flags = nullptr;       // bit0: reactant-1 name starts with 'G'; bit1: H2 photo sets NRH2;
                               // bit2: HD photo sets NRHD
+  // evaluation order: the reactions whose rate is a sum over the rays (the
+  // photo-reactions and photodesorption), grouped by kind, then the others,
+  // grouped by kind (lanes of a warp then mostly take the same branch)
+  int nray = 0, nother = 0;
+  int *ray_reac = nullptr;    // [nray]
+  int *other_reac = nullptr;  // [nother]
 };
 
 struct HostNet {

@@ -427,6 +427,19 @@ int build_device_tables(pdr_net *net) {
     net->rates.rtmin = upload(net, h.rtmin, rc);
     net->rates.rtmax = upload(net, h.rtmax, rc);
     net->rates.flags = upload(net, flags, rc);
+    std::vector<int> ray, other;
+    auto ray_kind = [](int k) {
+      return k == RK_PHOTO_H2 || k == RK_PHOTO_HD || k == RK_PHOTO_CO || k == RK_PHOTO_CI || k == RK_PHOTO_SI ||
+             k == RK_PHOTO || k == RK_PHOTD;
+    };
+    for (int i = 0; i < h.nreac; i++) (ray_kind(h.rate_kind[i]) ? ray : other).push_back(i);
+    auto by_kind = [&](int x, int y) { return h.rate_kind[x] < h.rate_kind[y]; };
+    std::stable_sort(ray.begin(), ray.end(), by_kind);
+    std::stable_sort(other.begin(), other.end(), by_kind);
+    net->rates.nray = (int)ray.size();
+    net->rates.nother = (int)other.size();
+    net->rates.ray_reac = upload(net, ray, rc);
+    net->rates.other_reac = upload(net, other, rc);
   }
   // ---- chemistry tables ----
   const int neq = h.neq;

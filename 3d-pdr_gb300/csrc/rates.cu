@@ -211,6 +211,62 @@ struct RateRow {
   int kind, dup, tail, flags;
 };
 
+// only the selected member of a duplicate group gets a rate (the member whose
+// temperature range holds T, else the group's last)
+__device__ __forceinline__ bool dup_selected(const RateRow *tab, int r, double t) {
+  const RateRow &w = tab[r];
+  if (w.dup > 0 && (w.kind == RK_THERMAL || w.kind == RK_PHOTO || w.kind == RK_CRP || w.kind == RK_CRPHOT)) {
+    int head = r;
+    while (head > 0 && tab[head].dup > 1) head--;
+    int sel = head;
+    while (!(t <= tab[sel].rtmax || tab[sel].tail)) sel++;
+    return sel == r;
+  }
+  return true;
+}
+
+// one ray's term of a ray-summed rate (the summand of calc_reac_rates.F90's
+// loop over the rays, the same expression in the same order)
+__device__ __forceinline__ double ray_term(const RateRow &w, double t, const double *rs, const double *av,
+                                           const double *cc, int ray, double dopw, double radw, int linear) {
+  const double a = w.alpha, g = w.gamma;
+  switch (w.kind) {
+    case RK_PHOTO_H2:
+    case RK_PHOTO_HD: {
+      const int c = (w.kind == RK_PHOTO_H2) ? 0 : 1;
+      return a * rs[ray] * h2shield1(cc[ray * 5 + c], dopw, radw) * scatter(av[ray], 1000.0, linear) / 2.0;
+    }
+    case RK_PHOTO_CO: {
+      const double nco = cc[ray * 5 + 2], nh2 = cc[ray * 5 + 0];
+      return a * rs[ray] * coshield(nco, nh2) * scatter(av[ray], lbar(nco, nh2), linear) / 2.0;
+    }
+    case RK_PHOTO_CI: {
+      const double tauc = g * av[ray] + 1.1e-17 * cc[ray * 5 + 3] +
+                          (0.9 * pow(t, 0.27) * pow(cc[ray * 5 + 0] / 1.59e21, 0.45));
+      return a * rs[ray] * exp(-tauc) / 2.0;
+    }
+    case RK_PHOTD: {
+      const double y = (t < 50.0) ? 3.5e-3 : (t < 85.0 ? 4.0e-3 : (t < 100.0 ? 5.5e-3 : 7.5e-3));
+      return 1.7e8 * rs[ray] * exp(-(1.8 * av[ray])) * 2.4e-22 * y;
+    }
+    default:   // RK_PHOTO, RK_PHOTO_SI
+      return a * rs[ray] * exp(-(g * av[ray])) / 2.0;
+  }
+}
+
+// calc_reac_rates.F90's clamps: a negative rate is reported, rates above 1
+// are capped unless the first reactant is a grain, rates below 1e-99 are zero
+__device__ __forceinline__ void store_rate(double k, const RateRow &w, int r, double *out, bool &neg, int &negr) {
+  if (k < 0.0) { negr = neg ? min(negr, r + 1) : r + 1; neg = true; }
+  if (k > 1.0 && !(w.flags & 1)) k = 1.0;
+  if (k < 1.0e-99) k = 0.0;
+  out[r] = k;
+}
+
+// One warp per cell.  The ray-summed reactions go first, one reaction per
+// group of nrays lanes (a lane per ray: the shielding functions of a ray run
+// in parallel, and the group's sum is taken in ray order); then the other
+// reactions, a lane each, in the order of their kinds.
 __global__ void __launch_bounds__(256) rates_kernel(const __grid_constant__ RateTables T, pdr_phys ph,
                                                     int ncell, int nrays, const double *__restrict__ Tg,
                                                     const double *__restrict__ Td,
@@ -235,6 +291,7 @@ __global__ void __launch_bounds__(256) rates_kernel(const __grid_constant__ Rate
   const int lane = threadIdx.x & 31;
   const int wpb = blockDim.x >> 5;
   const double dopw = ph.v_turb / (1000.0 * 1.0e-8), radw = 8.0e7;
+  const int linear = ph.xlambda_linear;
   for (int cell = blockIdx.x * wpb + (threadIdx.x >> 5); cell < ncell; cell += gridDim.x * wpb) {
     const double t = Tg[cell], td = Td[cell];
     // ZETA, or the cell's own rate in the cosmic-ray variant (zetacrlocal)
@@ -242,51 +299,42 @@ __global__ void __launch_bounds__(256) rates_kernel(const __grid_constant__ Rate
     const double *rs = rad + (size_t)cell * nrays;
     const double *av = AV + (size_t)cell * nrays;
     const double *cc = col5 + (size_t)cell * nrays * 5;
+    double *out = rate + (size_t)cell * nreac;
     bool neg = false;
     int negr = 0;
-    for (int r = lane; r < nreac; r += 32) {
-      const RateRow &w = tab[r];
-      // duplicate groups: only the selected member gets a rate
-      bool selected = true;
-      if (w.dup > 0 && (w.kind == RK_THERMAL || w.kind == RK_PHOTO || w.kind == RK_CRP || w.kind == RK_CRPHOT)) {
-        int head = r;
-        while (head > 0 && tab[head].dup > 1) head--;
-        int sel = head;
-        while (!(t <= tab[sel].rtmax || tab[sel].tail)) sel++;
-        selected = (sel == r);
+    if (nrays <= 32) {
+      const int per = 32 / nrays;
+      const int g = lane / nrays, ray = lane - g * nrays;
+      for (int base = 0; base < T.nray; base += per) {
+        const int j = base + g;
+        const bool act = (g < per) && (j < T.nray);
+        const int r = act ? __ldg(&T.ray_reac[j]) : 0;
+        double term = 0.0;
+        if (act && dup_selected(tab, r, t)) term = ray_term(tab[r], t, rs, av, cc, ray, dopw, radw, linear);
+        double k = 0.0;
+        for (int q = 0; q < nrays; q++) k = k + __shfl_sync(0xffffffffu, term, min(g * nrays + q, 31));
+        if (act && ray == 0) store_rate(k, tab[r], r, out, neg, negr);
       }
+    } else {
+      for (int j = lane; j < T.nray; j += 32) {
+        const int r = __ldg(&T.ray_reac[j]);
+        double k = 0.0;
+        if (dup_selected(tab, r, t))
+          for (int ray = 0; ray < nrays; ray++) k = k + ray_term(tab[r], t, rs, av, cc, ray, dopw, radw, linear);
+        store_rate(k, tab[r], r, out, neg, negr);
+      }
+    }
+    for (int i = lane; i < T.nother; i += 32) {
+      const int r = __ldg(&T.other_reac[i]);
+      const RateRow &w = tab[r];
       double k = 0.0;
-      if (selected) {
+      if (dup_selected(tab, r, t)) {
         const double a = w.alpha, b = w.beta, g = w.gamma;
         switch (w.kind) {
           case RK_H2FORM: k = ph.h2form ? h2_formation(t, td, ph.metallicity, ph.g2d) : 3.0e-18 * sqrt(t); break;
           case RK_PAH: k = a * pow(t / 100.0, b) * 0.4; break;
           case RK_THERMAL:
             k = (g < -200.0 && t < w.rtmin) ? 0.0 : a * pow(t / 300.0, b) * exp(-(g / t));
-            break;
-          case RK_PHOTO_H2:
-          case RK_PHOTO_HD: {
-            const int c = (w.kind == RK_PHOTO_H2) ? 0 : 1;
-            for (int ray = 0; ray < nrays; ray++)
-              k = k + a * rs[ray] * h2shield1(cc[ray * 5 + c], dopw, radw) * scatter(av[ray], 1000.0, ph.xlambda_linear) / 2.0;
-            break;
-          }
-          case RK_PHOTO_CO:
-            for (int ray = 0; ray < nrays; ray++) {
-              const double nco = cc[ray * 5 + 2], nh2 = cc[ray * 5 + 0];
-              k = k + a * rs[ray] * coshield(nco, nh2) * scatter(av[ray], lbar(nco, nh2), ph.xlambda_linear) / 2.0;
-            }
-            break;
-          case RK_PHOTO_CI:
-            for (int ray = 0; ray < nrays; ray++) {
-              const double tauc = g * av[ray] + 1.1e-17 * cc[ray * 5 + 3] +
-                                  (0.9 * pow(t, 0.27) * pow(cc[ray * 5 + 0] / 1.59e21, 0.45));
-              k = k + a * rs[ray] * exp(-tauc) / 2.0;
-            }
-            break;
-          case RK_PHOTO_SI:
-          case RK_PHOTO:
-            for (int ray = 0; ray < nrays; ray++) k = k + a * rs[ray] * exp(-(g * av[ray])) / 2.0;
             break;
           case RK_CRP: k = a * zeta; break;
           case RK_CRPHOT: k = a * zeta * pow(t / 300.0, b) * g / (1.0 - ph.omega); break;
@@ -297,21 +345,14 @@ __global__ void __launch_bounds__(256) rates_kernel(const __grid_constant__ Rate
             break;
           }
           case RK_CRH: k = 2.06e-3 * zeta * 2.4e-22 * ((g <= 1210.0) ? 1.0e5 : 0.0); break;
-          case RK_PHOTD: {
-            const double y = (t < 50.0) ? 3.5e-3 : (t < 85.0 ? 4.0e-3 : (t < 100.0 ? 5.5e-3 : 7.5e-3));
-            for (int ray = 0; ray < nrays; ray++) k = k + 1.7e8 * rs[ray] * exp(-(1.8 * av[ray])) * 2.4e-22 * y;
-            break;
-          }
           case RK_THERM: k = sqrt(2.0 * 1.5e15 * KB / (PI * PI * AU) * a / g) * exp(-(a / td)); break;
           case RK_GRAIN: k = a; break;
           default: k = 0.0; break;
         }
       }
-      if (k < 0.0) { neg = true; negr = r + 1; }
-      if (k > 1.0 && !(w.flags & 1)) k = 1.0;
-      if (k < 1.0e-99) k = 0.0;
-      rate[(size_t)cell * nreac + r] = k;
+      store_rate(k, w, r, out, neg, negr);
     }
+    // the lowest-numbered negative rate of the cell, as a negative status
     const unsigned anyneg = __ballot_sync(0xffffffffu, neg);
     if (status) {
       int rr = neg ? negr : 0x7fffffff;

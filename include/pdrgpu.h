@@ -225,7 +225,8 @@ int pdr_calculate_abundances(pdr_net *net, double *abundance, double *rate, doub
 /* ---- reaction rates: batched CALCULATE_REACTION_RATES (calc_reac_rates.F90:16-401) ----
  * d_rad_surface, d_AV: [ncell*nrays]; d_column5: [ncell*nrays*5] column
  * densities of H2, HD, CO, C, S along each ray; d_rate[ncell*nreac] out;
- * d_status[ncell]: 0, or -(reaction number) of a negative rate (the reference STOPs). */
+ * d_status[ncell]: 0, or -(the lowest reaction number with a negative rate; the
+ * reference STOPs there). */
 int pdr_rates_batched(const pdr_net *net, const pdr_phys *phys, int ncell, int nrays,
                       const double *d_T, const double *d_Td, const double *d_rad_surface,
                       const double *d_AV, const double *d_column5, double *d_rate, int *d_status,
