@@ -51,6 +51,7 @@ struct CoefShared {
   double rl1;     // 1/l[1]
   double tqd[6];
   float tqf[6], tauf[QMAX + 2];
+  float lf[QMAX + 1];   // l in FP32 (the mixed form's FP32 Nordsieck columns)
 };
 
 // coefficients of a uniform step history (xi_j = j), per order 1..5: the
@@ -60,6 +61,7 @@ struct CoefUniform {
   double url1[QMAX + 1];
   double utqd[QMAX + 1][6];
   float utqf[QMAX + 1][6];
+  float ulf[QMAX + 1][QMAX + 1];
 };
 
 // Comparisons of uniform FP64 scalars in integer arithmetic: for operands
@@ -131,6 +133,61 @@ struct ZShared {
   double *p;
   int s;
   __device__ __forceinline__ double &operator[](int j) const { return p[j * s]; }
+  __device__ __forceinline__ void bind(void *base, int lane, int stride) {
+    p = reinterpret_cast<double *>(base) + lane;
+    s = stride;
+  }
+};
+
+// Mixed-form Nordsieck row: the value y = z0 and the scaled first derivative
+// z1 = h y' in FP64 -- they enter the corrector equation directly -- and the
+// higher columns z2..z5 = h^j y^(j)/j! in FP32.  Those enter a step only
+// through the predicted z0 and z1, as terms of relative size (h/tau)^j for a
+// solution that varies on the time scale tau (error control at rtol 1e-8
+// holds h/tau near rtol^(1/(q+1)), so about 1e-3 of y and below at q >= 2):
+// their FP32 rounding moves the corrector's history term by ~1e-10 of y, about
+// 1 % of the local error the tolerance allows, while the corrector equation
+// itself (state, RHS, residual) stays FP64; the order heuristics read them
+// only through norms.  The prediction, correction and rescaling of z2..z5
+// then run on the FP32 pipe instead of the FP64 one.
+// Columns 0 and 1 are indexed by z[0], z[1]; columns 2..5 by getf/setf.
+struct ZRowM {
+  double v0, v1;
+  float f2, f3, f4, f5;
+  __device__ __forceinline__ double get(int j) const { return j == 0 ? v0 : v1; }
+  __device__ __forceinline__ void set(int j, double x) { if (j == 0) v0 = x; else v1 = x; }
+  __device__ __forceinline__ float getf(int j) const { return j == 2 ? f2 : j == 3 ? f3 : j == 4 ? f4 : f5; }
+  __device__ __forceinline__ void setf(int j, float x) {
+    if (j == 2) f2 = x; else if (j == 3) f3 = x; else if (j == 4) f4 = x; else f5 = x;
+  }
+  struct Ref {
+    ZRowM &r;
+    int j;
+    __device__ __forceinline__ operator double() const { return r.get(j); }
+    __device__ __forceinline__ Ref &operator=(double x) { r.set(j, x); return *this; }
+    __device__ __forceinline__ Ref &operator=(const Ref &o) { r.set(j, (double)o); return *this; }
+    __device__ __forceinline__ Ref &operator+=(double x) { r.set(j, r.get(j) + x); return *this; }
+    __device__ __forceinline__ Ref &operator-=(double x) { r.set(j, r.get(j) - x); return *this; }
+    __device__ __forceinline__ Ref &operator*=(double x) { r.set(j, r.get(j) * x); return *this; }
+  };
+  __device__ __forceinline__ Ref operator[](int j) { return Ref{*this, j}; }
+  __device__ __forceinline__ double operator[](int j) const { return get(j); }
+};
+
+// the same row in shared memory: z0, z1 at p[0], p[s]; z_j (j >= 2) at pf[(j-2)*s]
+struct ZSharedM {
+  double *p;
+  float *pf;
+  int s;
+  __device__ __forceinline__ double &operator[](int j) const { return p[j * s]; }
+  __device__ __forceinline__ float getf(int j) const { return pf[(j - 2) * s]; }
+  __device__ __forceinline__ void setf(int j, float x) const { pf[(j - 2) * s] = x; }
+  // base holds 2*stride doubles, then 4*stride floats
+  __device__ __forceinline__ void bind(void *base, int lane, int stride) {
+    p = reinterpret_cast<double *>(base) + lane;
+    pf = reinterpret_cast<float *>(reinterpret_cast<double *>(base) + 2 * stride) + lane;
+    s = stride;
+  }
 };
 
 // NORM32: the error weights, WRMS norms and the convergence-rate estimate in
@@ -144,7 +201,9 @@ struct Core {
   CoefShared *ws = nullptr;
   CoefUniform *wu = nullptr;   // the uniform-history table (may be shared by several integrators)
   // Nordsieck row of this thread's species, weight, correction, work values
-  typename std::conditional<ZSHARED, ZShared, ZRow>::type z;
+  using ZT = typename std::conditional<NORM32, typename std::conditional<ZSHARED, ZSharedM, ZRowM>::type,
+                                       typename std::conditional<ZSHARED, ZShared, ZRow>::type>::type;
+  ZT z;
   NT ewt;
   double acor, y, ftmp, tmp;
   // uniform integrator scalars
@@ -201,8 +260,84 @@ struct Core {
       for (int j = Q; j >= 1; j--)
         if (j >= k) z[j - 1] = (SIGN > 0) ? z[j - 1] + z[j] : z[j - 1] - z[j];
   }
+  // mixed form: the FP32 columns 2..Q take the Pascal triangle among
+  // themselves (their new values read only higher columns); z1 and z0 take
+  // S1 = sum j z_j and S0 = sum z_j over the FP32 columns -- of the columns
+  // before the update for the prediction, after it for the inverse -- in one
+  // FP64 add each: z0 <- z0 + z1 + S0, z1 <- z1 + S1, and back
+  template <int Q, int SIGN>
+  __device__ __forceinline__ void pascal_m() {
+    if constexpr (Q == 1) {
+      z[0] = (SIGN > 0) ? z[0] + z[1] : z[0] - z[1];
+    } else {
+      float s0 = 0.0f, s1 = 0.0f;
+      if constexpr (SIGN > 0) {
+#pragma unroll
+        for (int j = 2; j <= Q; j++) { const float f = z.getf(j); s0 += f; s1 = fmaf((float)j, f, s1); }
+      }
+#pragma unroll
+      for (int k = 1; k <= Q; k++)
+#pragma unroll
+        for (int j = Q; j >= 3; j--)
+          if (j >= k) z.setf(j - 1, (SIGN > 0) ? z.getf(j - 1) + z.getf(j) : z.getf(j - 1) - z.getf(j));
+      if constexpr (SIGN < 0) {
+#pragma unroll
+        for (int j = 2; j <= Q; j++) { const float f = z.getf(j); s0 += f; s1 = fmaf((float)j, f, s1); }
+      }
+      if constexpr (SIGN > 0) {
+        z[0] = z[0] + (z[1] + (double)s0);
+        z[1] = z[1] + (double)s1;
+      } else {
+        z[1] = z[1] - (double)s1;
+        z[0] = z[0] - (z[1] + (double)s0);
+      }
+    }
+  }
+  // the same with a run-time order, rolled (rows in shared memory)
+  template <int SIGN>
+  __device__ __forceinline__ void pascal_m_rolled() {
+    if (q == 1) {
+      z[0] = (SIGN > 0) ? z[0] + z[1] : z[0] - z[1];
+      return;
+    }
+    float s0 = 0.0f, s1 = 0.0f;
+    if (SIGN > 0) {
+#pragma unroll 1
+      for (int j = 2; j <= q; j++) { const float f = z.getf(j); s0 += f; s1 = fmaf((float)j, f, s1); }
+    }
+#pragma unroll 1
+    for (int k = 1; k <= q; k++)
+#pragma unroll 1
+      for (int j = q; j >= (k > 3 ? k : 3); j--)
+        z.setf(j - 1, (SIGN > 0) ? z.getf(j - 1) + z.getf(j) : z.getf(j - 1) - z.getf(j));
+    if (SIGN < 0) {
+#pragma unroll 1
+      for (int j = 2; j <= q; j++) { const float f = z.getf(j); s0 += f; s1 = fmaf((float)j, f, s1); }
+    }
+    if (SIGN > 0) {
+      z[0] = z[0] + (z[1] + (double)s0);
+      z[1] = z[1] + (double)s1;
+    } else {
+      z[1] = z[1] - (double)s1;
+      z[0] = z[0] - (z[1] + (double)s0);
+    }
+  }
   template <int SIGN>
   __device__ __forceinline__ void pascal_q() {
+    if constexpr (NORM32) {
+      if constexpr (ZSHARED) {
+        pascal_m_rolled<SIGN>();
+      } else {
+        switch (q) {
+          case 1: pascal_m<1, SIGN>(); break;
+          case 2: pascal_m<2, SIGN>(); break;
+          case 3: pascal_m<3, SIGN>(); break;
+          case 4: pascal_m<4, SIGN>(); break;
+          default: pascal_m<5, SIGN>(); break;
+        }
+      }
+      return;
+    }
     if constexpr (ZSHARED) {
       // rows in shared memory: a rolled loop keeps the step's code small
 #pragma unroll 1
@@ -223,17 +358,101 @@ struct Core {
   __device__ __forceinline__ void restore(double saved_t) { tn = saved_t; pascal_q<-1>(); }
 
   __device__ __forceinline__ void rescale() {
-    double fac = eta;
+    if constexpr (NORM32) {
+      z[1] = z[1] * eta;
+      const float ef = (float)eta;
+      float fac = ef * ef;
 #pragma unroll
-    for (int j = 1; j <= QMAX; j++)
-      if (j <= q) { z[j] *= fac; fac *= eta; }
+      for (int j = 2; j <= QMAX; j++)
+        if (j <= q) { z.setf(j, z.getf(j) * fac); fac *= ef; }
+    } else {
+      double fac = eta;
+#pragma unroll
+      for (int j = 1; j <= QMAX; j++)
+        if (j <= q) { z[j] *= fac; fac *= eta; }
+    }
     h = hscale * eta;
     hscale = h;
+  }
+
+  // a fresh row: y0 in column 0, zeros elsewhere
+  __device__ __forceinline__ void clear_row(double y0) {
+    z[0] = y0;
+    z[1] = 0.0;
+    if constexpr (NORM32) {
+#pragma unroll
+      for (int j = 2; j <= QMAX; j++) z.setf(j, 0.0f);
+    } else {
+#pragma unroll
+      for (int j = 2; j <= QMAX; j++) z[j] = 0.0;
+    }
+  }
+
+  // mixed form: the order changes below on the FP32 columns, with the
+  // coefficients from the FP32 step history
+  __device__ __forceinline__ void decrease_order_m() {
+    if (q <= 2) return;
+    float d[QMAX + 2];
+#pragma unroll
+    for (int j = 0; j < QMAX + 2; j++) d[j] = 0.0f;
+    d[2] = 1.0f;
+    const float hs = (float)hscale;
+    float hsum = 0.0f;
+#pragma unroll
+    for (int k = 1; k <= QMAX - 2; k++) {
+      if (k <= q - 2) {
+        hsum += ws->tauf[k];
+        const float xi = hsum / hs;
+#pragma unroll
+        for (int j = QMAX + 1; j >= 1; j--) d[j] = d[j - 1] + d[j] * xi;
+        d[0] *= xi;
+      }
+    }
+    float zq = 0.0f;
+#pragma unroll
+    for (int j = 2; j <= QMAX; j++) if (j == q) zq = z.getf(j);
+#pragma unroll
+    for (int j = 2; j < QMAX; j++)
+      if (j < q) z.setf(j, z.getf(j) - d[j] * zq);
+  }
+  __device__ __forceinline__ void increase_order_m() {
+    float d[QMAX + 2];
+#pragma unroll
+    for (int j = 0; j < QMAX + 2; j++) d[j] = 0.0f;
+    d[2] = 1.0f;
+    const float hs = (float)hscale;
+    float hsum = hs, sum_j = 1.0f, sum_xi = 1.0f, prod = 1.0f, xi_prev = 1.0f;
+#pragma unroll
+    for (int k = 2; k <= QMAX; k++) {
+      if (k <= q) {
+        hsum += ws->tauf[k];
+        const float xi = hsum / hs;
+        sum_j += 1.0f / k;
+        sum_xi += 1.0f / xi;
+        prod *= xi;
+#pragma unroll
+        for (int j = QMAX + 1; j >= 1; j--) d[j] = d[j - 1] + d[j] * xi_prev;
+        d[0] *= xi_prev;
+        xi_prev = xi;
+      }
+    }
+    const float c = (sum_j - sum_xi) / prod;
+    const float zn1 = c * z.getf(QMAX);
+#pragma unroll
+    for (int j = 2; j <= QMAX; j++)
+      if (j <= q) z.setf(j, z.getf(j) + d[j] * zn1);
+#pragma unroll
+    for (int j = 2; j <= QMAX; j++)
+      if (j == q + 1) z.setf(j, zn1);
   }
 
   // order q -> q-1: remove the x^q term keeping the value and slope at t_n and
   // the values at t_{n-1}..t_{n-q+2}: z_j -= d_j z_q, d = x^2 prod_{k<=q-2}(x+xi_k)
   __device__ __forceinline__ void decrease_order() {
+    if constexpr (NORM32) decrease_order_m();
+    else decrease_order_d();
+  }
+  __device__ __forceinline__ void decrease_order_d() {
     if (q <= 2) return;
     double d[QMAX + 2];
 #pragma unroll
@@ -261,6 +480,10 @@ struct Core {
   // order q -> q+1: add c x^2 prod_{k<q}(x+xi_k) so the polynomial also passes
   // through y_{n-q}; c = (sum_{j<=q} 1/j - sum_{i<=q} 1/xi_i)/prod_{i=2}^q xi_i * Delta_n
   __device__ __forceinline__ void increase_order() {
+    if constexpr (NORM32) increase_order_m();
+    else increase_order_d();
+  }
+  __device__ __forceinline__ void increase_order_d() {
     double d[QMAX + 2];
 #pragma unroll
     for (int j = 0; j < QMAX + 2; j++) d[j] = 0.0;
@@ -354,7 +577,10 @@ struct Core {
       coeffs<double>(qq, true, 1.0, one, l, tq);
       self().sync();
       if (self().leader()) {
-        for (int j = 0; j <= QMAX; j++) wu->ul[qq][j] = l[j];
+        for (int j = 0; j <= QMAX; j++) {
+          wu->ul[qq][j] = l[j];
+          wu->ulf[qq][j] = (float)l[j];
+        }
         wu->url1[qq] = 1.0 / l[1];
         for (int j = 1; j <= 5; j++) {
           wu->utqd[qq][j] = tq[j];
@@ -369,7 +595,10 @@ struct Core {
   template <int Q>
   __device__ __forceinline__ void store_l(const NT *l) {
 #pragma unroll
-    for (int j = 0; j <= Q; j++) ws->l[j] = (double)l[j];
+    for (int j = 0; j <= Q; j++) {
+      ws->l[j] = (double)l[j];
+      ws->lf[j] = (float)l[j];
+    }
   }
 
   __device__ __forceinline__ void set_coeffs() {
@@ -387,7 +616,10 @@ struct Core {
       else h_nt = h;
       if (self().leader()) {
 #pragma unroll
-        for (int j = 0; j <= QMAX; j++) ws->l[j] = wu->ul[q][j];
+        for (int j = 0; j <= QMAX; j++) {
+          ws->l[j] = wu->ul[q][j];
+          ws->lf[j] = wu->ulf[q][j];
+        }
         ws->rl1 = wu->url1[q];
         tq[2] = utqn(q, 2);
         tq[4] = utqn(q, 4);
@@ -575,7 +807,22 @@ struct Core {
       }
     }
     self().sync();
-    if constexpr (ZSHARED) {
+    // mixed form: the FP32 value of the correction for the FP32 columns, the
+    // order-raise save and the order heuristics
+    float acor32 = 0.0f;
+    if constexpr (NORM32) {
+      z[0] = fma(ws->l[0], acor, z[0]);
+      z[1] = fma(ws->l[1], acor, z[1]);
+      acor32 = (float)acor;
+      if constexpr (ZSHARED) {
+#pragma unroll 1
+        for (int j = 2; j <= q; j++) z.setf(j, fmaf(ws->lf[j], acor32, z.getf(j)));
+      } else {
+#pragma unroll
+        for (int j = 2; j <= QMAX; j++)
+          if (j <= q) z.setf(j, fmaf(ws->lf[j], acor32, z.getf(j)));
+      }
+    } else if constexpr (ZSHARED) {
 #pragma unroll 1
       for (int j = 0; j <= q; j++) z[j] = fma(ws->l[j], acor, z[j]);
     } else switch (q) {
@@ -585,7 +832,8 @@ struct Core {
     }
     qwait--;
     if (qwait == 1 && q != QMAX) {
-      z[QMAX] = acor;
+      if constexpr (NORM32) z.setf(QMAX, acor32);
+      else z[QMAX] = acor;
       saved_tq5 = tqn()[5];
     }
     if (eq_u(etamax, 1.0)) {
@@ -604,11 +852,18 @@ struct Core {
         qwait = 2;
         double etaqm1 = 0.0, etaqp1 = 0.0;
         if (q > 1) {
-          double zq = 0.0;
-#pragma unroll
-          for (int j = 0; j <= QMAX; j++) if (j == q) zq = z[j];
           const NT tq1 = tqn()[1];
-          etaqm1 = eta_of(wrms2(zq) * (tq1 * tq1), (float)BIAS1, q);
+          if constexpr (NORM32) {
+            float zq = 0.0f;
+#pragma unroll
+            for (int j = 2; j <= QMAX; j++) if (j == q) zq = z.getf(j);
+            etaqm1 = eta_of(wrms2_32(zq) * (tq1 * tq1), (float)BIAS1, q);
+          } else {
+            double zq = 0.0;
+#pragma unroll
+            for (int j = 0; j <= QMAX; j++) if (j == q) zq = z[j];
+            etaqm1 = eta_of(wrms2(zq) * (tq1 * tq1), (float)BIAS1, q);
+          }
         }
         if (q != QMAX && saved_tq5 != NT(0)) {
           // step-ratio factor of the order-raise estimate (heuristic, FP32)
@@ -617,16 +872,24 @@ struct Core {
           else ratio = (float)h / (float)ws->tau[2];
           float rp = ratio;
           for (int k = 1; k < L; k++) rp *= ratio;
-          const double cquot = (double)(((float)tqn()[5] / (float)saved_tq5) * rp);
+          const float cquot = ((float)tqn()[5] / (float)saved_tq5) * rp;
           const NT tq3 = tqn()[3];
-          etaqp1 = eta_of(wrms2(acor - cquot * z[QMAX]) * (tq3 * tq3), (float)BIAS3, L + 1);
+          if constexpr (NORM32)
+            etaqp1 = eta_of(wrms2_32(fmaf(-cquot, z.getf(QMAX), acor32)) * (tq3 * tq3), (float)BIAS3, L + 1);
+          else
+            etaqp1 = eta_of(wrms2(acor - (double)cquot * z[QMAX]) * (tq3 * tq3), (float)BIAS3, L + 1);
         }
         // ties keep the current order, then prefer the lower one
         const double etam = fmax(etaqm1, fmax(etaq, etaqp1));
         if (etam < THRESH) { eta = 1.0; qprime = q; }
         else if (etam == etaq) { eta = etaq; qprime = q; }
         else if (etam == etaqm1) { eta = etaqm1; qprime = q - 1; }
-        else { eta = etaqp1; qprime = q + 1; z[QMAX] = acor; }
+        else {
+          eta = etaqp1;
+          qprime = q + 1;
+          if constexpr (NORM32) z.setf(QMAX, acor32);
+          else z[QMAX] = acor;
+        }
         set_eta();
       }
     }
@@ -664,11 +927,22 @@ struct Core {
 
   __device__ __forceinline__ double interpolate(double t) const {
     const double s = (t - tn) / hscale;
-    double v = 0.0;
+    if constexpr (NORM32) {
+      // z0 + s (z1 + s (sum_{j>=2} s^(j-2) z_j)), the FP32 columns by Horner in FP32
+      if (q == 1) return fma(s, z[1], z[0]);
+      const float sf = (float)s;
+      float vf = 0.0f;
 #pragma unroll
-    for (int j = QMAX; j >= 0; j--)
-      if (j <= q) v = (j == q) ? z[j] : fma(s, v, z[j]);
-    return v;
+      for (int j = QMAX; j >= 2; j--)
+        if (j <= q) vf = (j == q) ? z.getf(j) : fmaf(sf, vf, z.getf(j));
+      return fma(s, fma(s, (double)vf, z[1]), z[0]);
+    } else {
+      double v = 0.0;
+#pragma unroll
+      for (int j = QMAX; j >= 0; j--)
+        if (j <= q) v = (j == q) ? z[j] : fma(s, v, z[j]);
+      return v;
+    }
   }
 
   // CVode(..., CV_NORMAL) from the current state to tout

@@ -895,9 +895,7 @@ struct CtaCell : Core<CtaCell<MIXED, SP>, false, MIXED> {
       sig[n] = 1.0f;
       sig[n + 1] = 0.0f;
     }
-#pragma unroll
-    for (int j = 0; j <= QMAX; j++) this->z[j] = 0.0;
-    this->z[0] = owns ? ab[tid] : 0.0;
+    this->clear_row(owns ? ab[tid] : 0.0);
     this->xe_last = ab[nspec - 1];
     __syncthreads();
     const double tend_yr = A.t_end_yr ? A.t_end_yr[cell] : A.t_end_default_yr;

@@ -90,7 +90,9 @@ __host__ __device__ inline WarpLayout warp_layout(int nsp, const WarpTables &T, 
   L.part = o; o += al(8 * (size_t)(T.nparts + 1));
   L.jrow = o; o += al((mixed ? 4 : 8) * (size_t)nsp * (nsp + 1));
   L.sig = o; o += al(4 * (size_t)(nsp + 2) + 4 * (size_t)nsp + 4 * (size_t)(nsp + 2));   // sig, perm, xs32
-  L.ws = o; o += al(sizeof(CoefShared) + (zsh ? 8 * (QMAX + 1) * kWarp : 0));
+  // the Nordsieck rows when they live in shared memory: six FP64 columns, or
+  // in the mixed form two FP64 and four FP32 columns
+  L.ws = o; o += al(sizeof(CoefShared) + (zsh ? (mixed ? 2 * 8 + 4 * 4 : 8 * (QMAX + 1)) * kWarp : 0));
   L.total = o;
   return L;
 }
@@ -454,9 +456,7 @@ struct WarpCell : Core<WarpCell<NSP, MIXED, ZSH>, ZSH, MIXED> {
     this->max_total_steps = A.max_total_steps;
     set_xe_coef();
     load_rates(A.rate + (size_t)cell * A.nreac, A.density[cell]);
-#pragma unroll
-    for (int j = 0; j <= QMAX; j++) this->z[j] = 0.0;
-    this->z[0] = owns ? ab[lane] : 0.0;
+    this->clear_row(owns ? ab[lane] : 0.0);
     this->xe_last = ab[nspec - 1];
     const double tend_yr = A.t_end_yr ? A.t_end_yr[cell] : A.t_end_default_yr;
     double yv = 0.0;
@@ -504,10 +504,7 @@ __global__ void __launch_bounds__(RegVariant<RV>::threads, RegVariant<RV>::min_b
   const WarpLayout L = warp_layout(NSP, A.tab, MIXED, ZSH);
   WarpCell<NSP, MIXED, ZSH> c(A, lane);
   c.bind(smem_raw + L.total * warp, L);
-  if constexpr (ZSH) {
-    c.z.p = reinterpret_cast<double *>(reinterpret_cast<unsigned char *>(c.ws) + sizeof(CoefShared)) + lane;
-    c.z.s = kWarp;
-  }
+  if constexpr (ZSH) c.z.bind(reinterpret_cast<unsigned char *>(c.ws) + sizeof(CoefShared), lane, kWarp);
   // the uniform-history coefficient table, one copy per block
   __shared__ CoefUniform uni;
   c.wu = &uni;
