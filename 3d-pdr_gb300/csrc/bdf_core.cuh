@@ -230,15 +230,17 @@ struct Core {
     else return ws->tau;
   }
 
+  float inv_n32 = 0.0f;   // 1/n in FP32, set at the start of integrate()
   __device__ __forceinline__ NT wrms2(double v) {
     const NT t = self().owns ? (NT)v * ewt : NT(0);
-    return self().sum_all(t * t) * (NT)self().inv_n;
+    if constexpr (NORM32) return self().sum_all(t * t) * inv_n32;
+    else return self().sum_all(t * t) * (NT)self().inv_n;
   }
   // the same norm of a value already held in FP32 (the mixed form's Newton
   // correction comes out of the FP32 solve): no conversion
   __device__ __forceinline__ float wrms2_32(float v) {
     const float t = self().owns ? v * ewt : 0.0f;
-    return self().sum_all(t * t) * (float)self().inv_n;
+    return self().sum_all(t * t) * inv_n32;
   }
 
   // FP32 copies of the tolerances (mixed form), set at the start of integrate()
@@ -986,6 +988,7 @@ struct Core {
     self().sync();
     rtol32 = (float)rtol;
     atol32 = (float)atol;
+    inv_n32 = (float)self().inv_n;
     nfe = nje = nsetups = nni = ncfn = netf = 0;
     nst = nstlp = 0;
     saved_tq5 = NT(0);

@@ -356,10 +356,10 @@ struct CtaCell : Core<CtaCell<MIXED, SP>, false, MIXED> {
       MT s = MT(0);
 #pragma unroll 4
       for (int t = 0; t < T.hlen; t++) {
-        const int x = __ldg(&T.h_x[t * G + tid]);
-        const int y = __ldg(&T.h_y[t * G + tid]);
+        const int2 xy = __ldg(&T.h_xy[t * G + tid]);
+        const int x = xy.x, y = xy.y;
         MT nu;
-        if constexpr (MIXED) nu = __ldg(&T.h_nu_f[t * G + tid]);
+        if constexpr (MIXED) nu = (MT)(x >> 19);
         else nu = __ldg(&T.h_nu[t * G + tid]);
         const int r = x & 0xffff;
         s = fma(nu, (x & 0x10000) ? Db[r] : Da[r], s);
@@ -387,7 +387,9 @@ struct CtaCell : Core<CtaCell<MIXED, SP>, false, MIXED> {
       if constexpr (MIXED) rf = (MT)rf_d * (wsc32 * this->atol32);
       else rf = (MT)rf_d;
       for (int j = 0; j < n; j++) {
-        const MT cj = (MT)__ldg(&T.xe_coef[j]);
+        MT cj;
+        if constexpr (MIXED) cj = __ldg(&T.xe_coef_f[j]);
+        else cj = __ldg(&T.xe_coef[j]);
         MT v = M(tid, j);
         if constexpr (MIXED) v = fmaf(e * cj, sig[j], v);
         else v = fma(e, cj, v);
@@ -637,9 +639,9 @@ struct CtaCell : Core<CtaCell<MIXED, SP>, false, MIXED> {
       MT s = MT(0);
 #pragma unroll 4
       for (int t = 0; t < T.hlen; t++) {
-        const int x = __ldg(&T.h_x[t * G + tid]);
-        const int y = __ldg(&T.h_y[t * G + tid]);
-        const MT nu = __ldg(&T.h_nu_f[t * G + tid]);
+        const int2 xy = __ldg(&T.h_xy[t * G + tid]);
+        const int x = xy.x, y = xy.y;
+        const MT nu = (MT)(x >> 19);
         const int r = x & 0xffff;
         s = fma(nu, (x & 0x10000) ? Db[r] : Da[r], s);
         const int kind = (x >> 17) & 3;

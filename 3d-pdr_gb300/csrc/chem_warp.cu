@@ -378,10 +378,10 @@ struct WarpCell : Core<WarpCell<NSP, MIXED, ZSH>, ZSH, MIXED> {
       MT s = MT(0);
 #pragma unroll 2
       for (int t = 0; t < T.hlen; t++) {
-        const int x = __ldg(&T.h_x[t * kWarp + lane]);
-        const int y = __ldg(&T.h_y[t * kWarp + lane]);
+        const int2 xy = __ldg(&T.h_xy[t * kWarp + lane]);
+        const int x = xy.x, y = xy.y;
         MT nu;
-        if constexpr (MIXED) nu = __ldg(&T.h_nu_f[t * kWarp + lane]);
+        if constexpr (MIXED) nu = (MT)(x >> 19);
         else nu = __ldg(&T.h_nu[t * kWarp + lane]);
         const int r = x & 0xffff;
         s = fma(nu, (x & 0x10000) ? Db[r] : Da[r], s);
@@ -409,7 +409,9 @@ struct WarpCell : Core<WarpCell<NSP, MIXED, ZSH>, ZSH, MIXED> {
     else rf = (MT)rf_d;
 #pragma unroll 4
     for (int j = 0; j < NSP; j++) {
-      const MT cj = (MT)__ldg(&T.xe_coef[j]);
+      MT cj;
+      if constexpr (MIXED) cj = __ldg(&T.xe_coef_f[j]);
+      else cj = __ldg(&T.xe_coef[j]);
       MT v = owns ? row[j] : MT(0);
       if constexpr (MIXED) v = fmaf(e * cj, sig[j], v);
       else v = fma(e, cj, v);

@@ -55,6 +55,7 @@ struct WarpTables {
   double *jac_nu = nullptr;   // [jac_len][lanes]
   float *jac_nu_f = nullptr;  // [jac_len][lanes]
   double *xe_coef = nullptr;  // [lanes] electron-sum coefficient per slot
+  float *xe_coef_f = nullptr; // the same in FP32 (the mixed forms' Newton matrix)
   // term-parallel Jacobian assembly (block integrator): the (row, column)
   // contributions nu * dphi_r/dx_col of every term, sorted by entry and cut
   // into `lanes` balanced chunks; a chunk sums each run of one entry in a
@@ -62,10 +63,11 @@ struct WarpTables {
   // boundary, leaves its partial in a boundary slot (kind 2) that a second
   // pass adds up in chunk order
   int hlen = 0, nbnd = 0;
-  int *h_x = nullptr;         // [hlen][lanes] reaction | Db? << 16 | kind << 17 (0 accumulate, 1 store, 2 slot)
-  int *h_y = nullptr;         // [hlen][lanes] row | column << 8 | slot << 16
-  double *h_nu = nullptr;     // [hlen][lanes] nu (0 = padding)
-  float *h_nu_f = nullptr;
+  // [hlen][lanes] one 8-byte load per contribution:
+  //   .x = reaction | Db? << 16 | kind << 17 (0 accumulate, 1 store, 2 slot) | nu << 19 (signed, 0 = padding)
+  //   .y = row | column << 8 | slot << 16
+  int2 *h_xy = nullptr;
+  double *h_nu = nullptr;     // [hlen][lanes] nu as FP64 (the FP64 forms: no integer conversion on the FP64 pipe)
   int *bnd_t = nullptr;       // [nbnd] row | column << 8 | sparse location << 16 of a boundary entry
   int *bnd_s = nullptr;       // [nbnd] first slot | (last slot + 1) << 16
   // Sparse Newton matrix of the block integrator's mixed form (sp.ok): the
@@ -77,7 +79,7 @@ struct WarpTables {
   // level at a time; the last m = N - a rows, nearly dense after fill, hold
   // their leaf-column part packed and their trailing m x m block dense
   // (column-major, stride ldb), factorised with partial pivoting.  For a
-  // kind-1 term entry the high 16 bits of h_y hold its location in the
+  // kind-1 term entry the high 16 bits of h_xy.y hold its location in the
   // storage, for a boundary entry those of bnd_t.
   struct Sparse {
     int ok = 0;

@@ -598,10 +598,10 @@ int build_device_tables(pdr_net *net) {
     std::vector<double> xe(G, 0.0);
     for (int i = 0; i < neq; i++) xe[i] = h.xe[i];
     // term-parallel Jacobian tables (both integrators)
-    std::vector<int> hx, hy, bt, bs;
+    std::vector<int2> hxy;
+    std::vector<int> bt, bs;
     SparsePlan plan;
     std::vector<double> hn;
-    std::vector<float> hnf;
     {
       struct Half { int i, col, r, which; double nu; };
       std::vector<Half> hs;
@@ -630,10 +630,8 @@ int build_device_tables(pdr_net *net) {
         return l < 0 ? 0u : (unsigned)l;
       };
       w.hlen = std::max(1, (H + G - 1) / G);
-      hx.assign((size_t)w.hlen * G, 0);
-      hy.assign((size_t)w.hlen * G, 0);
+      hxy.assign((size_t)w.hlen * G, int2{0, 0});
       hn.assign((size_t)w.hlen * G, 0.0);
-      hnf.assign((size_t)w.hlen * G, 0.0f);
       // an entry's runs: the chunks holding it, in order
       int slot = 0;
       for (int e0 = 0; e0 < H;) {
@@ -650,12 +648,15 @@ int build_device_tables(pdr_net *net) {
               kind = (c0 == c1) ? 1 : 2;
               if (kind == 2) sl = slot++;
             }
-            hx[(size_t)t * G + c] = hs[k].r | (hs[k].which << 16) | (kind << 17);
+            // nu, a stoichiometric count, rides in the high bits as a signed integer
+            const int nu_i = (int)hs[k].nu;
+            if ((double)nu_i != hs[k].nu || nu_i < -4096 || nu_i > 4095 || hs[k].r > 0xffff) return PDR_E_NET;
+            hxy[(size_t)t * G + c].x = (int)((unsigned)hs[k].r | ((unsigned)hs[k].which << 16) | ((unsigned)kind << 17) |
+                                             ((unsigned)nu_i << 19));
             // kind 1 (a store): the entry's sparse location; kind 2: its slot
             const unsigned hi = (kind == 1) ? sp_loc(hs[k].i, hs[k].col) : (unsigned)sl;
-            hy[(size_t)t * G + c] = (int)((unsigned)hs[k].i | ((unsigned)hs[k].col << 8) | (hi << 16));
+            hxy[(size_t)t * G + c].y = (int)((unsigned)hs[k].i | ((unsigned)hs[k].col << 8) | (hi << 16));
             hn[(size_t)t * G + c] = hs[k].nu;
-            hnf[(size_t)t * G + c] = (float)hs[k].nu;
           }
         }
         if (c0 != c1) {
@@ -685,10 +686,12 @@ int build_device_tables(pdr_net *net) {
     w.jac_nu_f = upload(net, jnf, rc2);
     w.xe_coef = upload(net, xe, rc2);
     {
-      w.h_x = upload(net, hx, rc2);
-      w.h_y = upload(net, hy, rc2);
+      std::vector<float> xef(xe.begin(), xe.end());
+      w.xe_coef_f = upload(net, xef, rc2);
+    }
+    {
+      w.h_xy = upload(net, hxy, rc2);
       w.h_nu = upload(net, hn, rc2);
-      w.h_nu_f = upload(net, hnf, rc2);
       if (!bt.empty()) {
         w.bnd_t = upload(net, bt, rc2);
         w.bnd_s = upload(net, bs, rc2);

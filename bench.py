@@ -46,7 +46,7 @@ CONFIGS = {"C1": dict(network="reduced", ncell=64, seed=1001,
            "C2": dict(network="full", ncell=32768, seed=1002,
                       text="full network, 32^3 = 32768 cells (C2), t_end 1e7 yr, rtol 1e-8, atol 1e-30")}
 FALLBACK_HBM_GBS = 6800.0
-CASES = ["rates", "heating", "lte-CO", "levpop-CII", "levpop-CO", "columns", "tau", "thermal", "levconv"]
+CASES = ["rates", "rates-full", "heating", "lte-CO", "levpop-CII", "levpop-CO", "columns", "tau", "thermal", "levconv"]
 
 
 def parse():
@@ -596,14 +596,15 @@ def kernel_case(a):
     stream = torch.cuda.Stream(device=dev)
     name = a.case
     d = lambda x: torch.as_tensor(np.ascontiguousarray(x), device=dev)
-    if name in ("rates", "heating"):
+    if name in ("rates", "rates-full", "heating"):
         n = a.ncell or 262144
-        w = W.chemistry("C3", ncell=n, seed=CONFIGS["C3"]["seed"])
-        net = G.Network("reduced")
+        cfg = "C2" if name == "rates-full" else "C3"
+        w = W.chemistry(cfg, ncell=n, seed=CONFIGS[cfg]["seed"])
+        net = G.Network(CONFIGS[cfg]["network"])
         ph = G.phys(w.zeta, w.omega, w.grain_radius, w.metallicity, w.g2d, w.v_turb_kms)
         args = [d(w.T), d(w.Td), d(w.rad_surface), d(w.AV), d(w.column5)]
         rate, _ = G.reaction_rates(net, ph, *args, stream=stream)
-        if name == "rates":
+        if name != "heating":
             fn = lambda: G.reaction_rates(net, ph, *args, rate=rate, stream=stream)
         else:
             ab = d(np.tile(W.initial_abundances(net.species), (n, 1)))
