@@ -180,6 +180,68 @@ __device__ __forceinline__ bool refine_ok(double ax, double as, double prev, dou
   return true;
 }
 
+// The mixed solve's FP32 inverse of the row-equilibrated matrix: Gauss-Jordan
+// with partial pivoting (the largest |a_ik| among the rows not yet pivoted,
+// lowest row on ties), in place.  The inverse only preconditions the FP64
+// refinement, so it need not follow the reference's full-pivot order, and a
+// column search costs two compares per lane where the full search scans the
+// matrix.  Lanes own columns (l = lane, lane + 32); the rows are a uniform
+// loop, so no element index is divided.  dumv: n floats.  Returns false on a
+// zero pivot.
+__device__ bool gj_inverse_pp(float *a, int n, float *dumv, int *indxr) {
+  const int lane = threadIdx.x & 31;
+  const int l0 = lane, l1 = lane + 32;
+  for (int k = 0; k < n; k++) {
+    float best = -1.0f;
+    int bi = n;
+    for (int i = k + lane; i < n; i += 32) {
+      const float v = fabsf(a[i * n + k]);
+      if (v > best) { best = v; bi = i; }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float ov = __shfl_xor_sync(FULL, best, o);
+      const int oi = __shfl_xor_sync(FULL, bi, o);
+      if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
+    }
+    if (!(best > 0.0f)) return false;
+    if (bi != k) {
+      if (l0 < n) { const float t = a[bi * n + l0]; a[bi * n + l0] = a[k * n + l0]; a[k * n + l0] = t; }
+      if (l1 < n) { const float t = a[bi * n + l1]; a[bi * n + l1] = a[k * n + l1]; a[k * n + l1] = t; }
+    }
+    if (lane == 0) indxr[k] = bi;
+    __syncwarp();
+    const float pivinv = 1.0f / a[k * n + k];
+    // the multipliers of column k, read before any row changes
+    for (int i = lane; i < n; i += 32) dumv[i] = a[i * n + k];
+    __syncwarp();
+    // pivot row scaled (its column k becomes 1/pivot); the other rows take
+    // a_il -= a_kl a_ik, column k from zero
+    float p0 = 0.0f, p1 = 0.0f;
+    if (l0 < n) { p0 = (l0 == k) ? pivinv : a[k * n + l0] * pivinv; a[k * n + l0] = p0; }
+    if (l1 < n) { p1 = (l1 == k) ? pivinv : a[k * n + l1] * pivinv; a[k * n + l1] = p1; }
+    for (int i = 0; i < n; i++) {
+      if (i == k) continue;
+      const float dum = dumv[i];
+      if (l0 < n) a[i * n + l0] = fmaf(-p0, dum, (l0 == k) ? 0.0f : a[i * n + l0]);
+      if (l1 < n) a[i * n + l1] = fmaf(-p1, dum, (l1 == k) ? 0.0f : a[i * n + l1]);
+    }
+    __syncwarp();
+  }
+  // the row interchanges undone on the inverse's columns, last first
+  for (int k = n - 1; k >= 0; k--) {
+    const int r = indxr[k];
+    if (r != k)
+      for (int i = lane; i < n; i += 32) {
+        const float t = a[i * n + r];
+        a[i * n + r] = a[i * n + k];
+        a[i * n + k] = t;
+      }
+    __syncwarp();
+  }
+  return true;
+}
+
 template <bool MIXED>
 __global__ void __launch_bounds__(256) levpop_kernel(const __grid_constant__ CoolantTables C,
                                                      const __grid_constant__ LevArgs A) {
@@ -318,48 +380,56 @@ __global__ void __launch_bounds__(256) levpop_kernel(const __grid_constant__ Coo
       ok = gauss_jordan<double>(R, b, n, rs, indxr, indxc, false);
       for (int i = lane; i < n; i += 32) x[i] = b[i];
     } else {
-      // rows equilibrated by their largest entry, FP32 Gauss-Jordan inverse of
-      // D M, then x = inv D b and up to two FP64 refinement steps
-      // x += inv D (b - M x), each accepted by the size of the correction the
-      // next step would make (refine_ok); otherwise the cell is re-solved by
-      // the FP64 Gauss-Jordan (R is intact)
+      // FP32 copy of the matrix with its rows equilibrated in FP32 (D M, D =
+      // 1 / row maximum), the FP32 inverse of D M (partial pivoting), then
+      // x = inv(DM) D b and up to two refinement steps x += inv(DM) D (b - M x)
+      // with the residual in FP64 and the correction in FP32.  Each step is
+      // accepted by the size of the correction the next would make
+      // (refine_ok); otherwise the cell is re-solved by the FP64
+      // Gauss-Jordan (R is intact).
       float *Mf = reinterpret_cast<float *>(base + L.Mf);
-      float *bf = Mf + nn;
-      for (int i = lane; i < n; i += 32) {
-        double mx = 0.0;
-        for (int l = 0; l < n; l++) mx = fmax(mx, fabs(R[i * n + l]));
-        rs[i] = (mx > 0.0) ? 1.0 / mx : 1.0;
-      }
-      __syncwarp();
-      for (int e = lane; e < nn; e += 32) Mf[e] = (float)(R[e] * rs[e / n]);
-      for (int i = lane; i < n; i += 32) bf[i] = 0.0f;
-      __syncwarp();
-      ok = gauss_jordan<float>(Mf, bf, n, reinterpret_cast<float *>(ipiv), indxr, indxc, true);   // Mf := inverse of D M
+      float *rf = Mf + nn;                            // FP32 scaled residual
+      float *rsf = reinterpret_cast<float *>(rs);     // FP32 row scales
+      float *prev = reinterpret_cast<float *>(sp);    // |previous correction| (s_pop is no longer needed)
+      float *dumv = reinterpret_cast<float *>(ipiv);
+      for (int e = lane; e < nn; e += 32) Mf[e] = (float)R[e];
       __syncwarp();
       for (int i = lane; i < n; i += 32) {
-        double s = 0.0;
-        for (int l = 0; l < n; l++) s = fma((double)Mf[i * n + l], rs[l] * b[l], s);
-        x[i] = s;
+        float mx = 0.0f;
+        for (int l = 0; l < n; l++) mx = fmaxf(mx, fabsf(Mf[i * n + l]));
+        rsf[i] = (mx > 0.0f) ? 1.0f / mx : 1.0f;
       }
+      __syncwarp();
+      for (int i = 0; i < n; i++) {
+        const float r = rsf[i];
+        for (int l = lane; l < n; l += 32) Mf[i * n + l] *= r;
+      }
+      __syncwarp();
+      ok = gj_inverse_pp(Mf, n, dumv, indxr);
+      __syncwarp();
+      // b is zero but for its last entry: x = column n-1 of the inverse times D b
+      const double bl = b[n - 1] * (double)rsf[n - 1];
+      for (int i = lane; i < n; i += 32) x[i] = (double)Mf[i * n + n - 1] * bl;
       bool good = false;
       for (int it = 0; it < 3 && ok && !good; it++) {
         __syncwarp();
         for (int i = lane; i < n; i += 32) {
           double s = b[i];
           for (int l = 0; l < n; l++) s = fma(-R[i * n + l], x[l], s);
-          sp[i] = s * rs[i];   // scaled residual (s_pop is no longer needed)
+          rf[i] = (float)s * rsf[i];
         }
         __syncwarp();
         bool bad = false;
         for (int i = lane; i < n; i += 32) {
-          double s = 0.0;
-          for (int l = 0; l < n; l++) s = fma((double)Mf[i * n + l], sp[l], s);
+          float s32 = 0.0f;
+          for (int l = 0; l < n; l++) s32 = fmaf(Mf[i * n + l], rf[l], s32);
+          const double s = (double)s32;
           // from the second correction on, the correction is also the test of
           // the previous one
-          if (it > 0 && !refine_ok(fabs(x[i]), fabs(s), (double)bf[i], dens)) bad = true;
+          if (it > 0 && !refine_ok(fabs(x[i]), fabs(s), (double)prev[i], dens)) bad = true;
           if (it < 2) {
             x[i] += s;
-            bf[i] = (float)fabs(s);
+            prev[i] = fabsf(s32);
           }
         }
         good = (it > 0) && !__any_sync(FULL, bad);
