@@ -18,7 +18,10 @@
 //     launches in flight, and those are told to shrink to that share
 //     (pdr_solver_limit_sms, a 4-byte copy on a control stream): their blocks
 //     beyond it stop taking cells at the next cell boundary and the hardware
-//     hands those SMs to the new launch;
+//     hands those SMs to the new launch.  A persistent launch cannot widen its
+//     grid again, so a batch is solved in chunks of about sixteen waves, each
+//     launched with the share of the moment: once the newcomers finish, the
+//     next chunk takes their SMs back;
 //   * admission by device-memory footprint: requests whose bytes (inputs, rate
 //     constants, outputs per cell) would push the admitted-and-unfinished total
 //     over the budget are refused with PDR_E_BUSY.
@@ -68,6 +71,7 @@ struct Lane {
   pdr_net *net = nullptr;
   int nspec = 0, nreac = 0;
   double cell_bytes = 0.0;
+  int cells_per_sm = 0;   // cells one SM holds at once (16 warps, or 2 blocks of the block integrator)
   std::vector<std::unique_ptr<Slot>> slots;
   std::deque<Req *> queue;
   long long batches = 0, cells = 0;
@@ -127,7 +131,9 @@ void free_slot(Slot &S) {
   if (S.stream) cudaStreamDestroy(S.stream);
 }
 
-// one launch over the packed requests: rates, then the batched solve
+int claim_sms(pdr_server *s, Slot &me, bool counted = false);
+
+// the packed requests: rates, then the batched solve
 int run_batch(pdr_server *s, Lane &L, Slot &S, const std::vector<Req *> &batch) {
   const int nr = s->opts.nrays;
   size_t off = 0;
@@ -162,7 +168,21 @@ int run_batch(pdr_server *s, Lane &L, Slot &S, const std::vector<Req *> &batch) 
   int rc = pdr_rates_batched(L.net, &s->phys, n, nr, S.d_T, S.d_Td, S.d_rad, S.d_AV, S.d_col, S.d_rate, S.d_rstatus,
                              st);
   if (rc) return rc;
-  rc = pdr_solver_run(S.solver, n, S.d_ab, S.d_rate, S.d_nH, S.d_tend, S.d_status, nullptr, st);
+  // the solve in chunks of about sixteen waves at the slot's share
+  for (int c0 = 0; c0 < n && !rc;) {
+    int m = n - c0;
+    if (c0 > 0 && s->opts.partition_sms) {
+      std::lock_guard<std::mutex> lk(s->mu);
+      const int share = claim_sms(s, S, true);
+      pdr_solver_set_max_sms(S.solver, share);
+    }
+    // (a slot outside slot_loop -- the warm-up at creation -- has no share yet:
+    // it counts as the whole device; every chunk holds at least one cell)
+    if (s->opts.partition_sms) m = std::min(m, std::max(1, 16 * (S.share > 0 ? S.share : s->sms) * L.cells_per_sm));
+    rc = pdr_solver_run(S.solver, m, S.d_ab + (size_t)c0 * L.nspec, S.d_rate + (size_t)c0 * L.nreac, S.d_nH + c0,
+                        S.d_tend + c0, S.d_status + c0, nullptr, st);
+    c0 += m;
+  }
   if (rc) return rc;
   if ((e = cudaMemcpyAsync(S.h_ab, S.d_ab, 8 * (size_t)n * L.nspec, cudaMemcpyDeviceToHost, st)) ||
       (e = cudaMemcpyAsync(S.h_status, S.d_status, 4 * (size_t)n, cudaMemcpyDeviceToHost, st)) ||
@@ -185,9 +205,10 @@ int run_batch(pdr_server *s, Lane &L, Slot &S, const std::vector<Req *> &batch) 
 
 // Called with the server lock held: the SMs of a launch that is about to
 // start, and the shrinking of the launches in flight to the same share.
-int claim_sms(pdr_server *s, Slot &me) {
+// `counted`: this slot is already among the running ones (a later chunk).
+int claim_sms(pdr_server *s, Slot &me, bool counted) {
   if (!s->opts.partition_sms) return 0;
-  const int share = std::max(1, s->sms / (s->running + 1));
+  const int share = std::max(1, s->sms / std::max(1, s->running + (counted ? 0 : 1)));
   for (Lane &L : s->lanes)
     for (auto &sp : L.slots) {
       Slot &o = *sp;
@@ -287,6 +308,12 @@ int pdr_server_create(pdr_net *const *nets, int nnet, const pdr_phys *phys, cons
     // device bytes per cell: n_H, T, T_dust, end time, per-ray field, A_V and
     // five columns, abundances, rate constants, two status words
     L.cell_bytes = 8.0 * (4 + 7 * nr + L.nspec + L.nreac) + 8.0;
+    {
+      pdr_chem_opts o;
+      pdr_chem_opts_default(&o);
+      o.precision = s->opts.precision;
+      L.cells_per_sm = pdr::uses_warp_path(L.net, o) ? 16 : 2;
+    }
     for (int k = 0; k < s->opts.slots_per_lane && !rc; k++) {
       L.slots.emplace_back(new Slot());
       rc = alloc_slot(s, L, *L.slots.back());

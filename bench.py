@@ -412,14 +412,17 @@ def level_population_grid(G, W, dev, stream):
     return out
 
 
-def served_stream(G, W, nreq_reduced=500, rate_reduced=12.0, nreq_mix=20, rate_mix=0.4):
+def served_stream(G, W, nreq_reduced=500, rate_reduced=12.0, nreq_mix=100, rate_mix=0.8):
     """C5: requests replayed at Poisson arrival times into the serving loop
     (pdr_server_*: per-network lanes with launch slots, SM sharing, admission
     by device-memory footprint); blocks of logU(1, 50000) cells with C1
     conditions, t_end logU(1e4, 1e7) yr.  The configuration's 200 requests/s
     (about 0.9 M cells/s offered, a fifth of it full-network) exceed one GPU,
     so the streams are replayed at rates the GPU sustains: 500 reduced-network
-    requests at 12/s, and the 80 % reduced / 20 % full mix at 0.4/s."""
+    requests at 12/s, and 100 requests of the 80 % reduced / 20 % full mix at
+    0.8/s (a full-network request of n cells holds the whole GPU for about
+    n / 2,800 s; at 1.35/s the same stream took 107 s to serve 74 s of
+    arrivals, so latency measured the queue)."""
     out = {"workload": "Poisson arrivals, blocks logU(1, 50000) cells, t_end logU(1e4, 1e7) yr, "
                        "C1 cell conditions (C5)"}
     w0 = W.chemistry("C1", ncell=1)
