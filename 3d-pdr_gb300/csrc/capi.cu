@@ -480,16 +480,23 @@ int pdr_chem_autotune(const pdr_net *net, int ncell_sample, const double *d_abun
     o.reg_variant = c.reg;
     o.refill = c.refill;
     o.blocks_per_sm = 0;
-    e = cudaMemcpyAsync(ab, d_abundance, sizeof(double) * (size_t)ncell_sample * ns, cudaMemcpyDeviceToDevice, st);
-    if (e != cudaSuccess) { rc = cuda_fail(e, "autotune copy"); break; }
-    cudaEventRecord(t0, st);
-    rc = pdr_chem_solve_batched(net, ncell_sample, ab, d_rate, d_density, nullptr, &o, status, nullptr, st);
+    // the best of two timed runs: the first of a shape also pays its
+    // one-time kernel-attribute and occupancy set-up
+    float ms = 1e30f;
+    for (int rep = 0; rep < 2 && rc == 0; rep++) {
+      e = cudaMemcpyAsync(ab, d_abundance, sizeof(double) * (size_t)ncell_sample * ns, cudaMemcpyDeviceToDevice, st);
+      if (e != cudaSuccess) { rc = cuda_fail(e, "autotune copy"); break; }
+      cudaEventRecord(t0, st);
+      rc = pdr_chem_solve_batched(net, ncell_sample, ab, d_rate, d_density, nullptr, &o, status, nullptr, st);
+      if (rc) break;
+      cudaEventRecord(t1, st);
+      e = cudaEventSynchronize(t1);
+      if (e != cudaSuccess) { rc = cuda_fail(e, "autotune run"); break; }
+      float t = 0.f;
+      cudaEventElapsedTime(&t, t0, t1);
+      if (t < ms) ms = t;
+    }
     if (rc) break;
-    cudaEventRecord(t1, st);
-    e = cudaEventSynchronize(t1);
-    if (e != cudaSuccess) { rc = cuda_fail(e, "autotune run"); break; }
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, t0, t1);
     if (log)
       fprintf(stderr, "pdr_chem_autotune: warps_per_block %d reg_variant %d refill %d: %.3f ms\n", c.wpb, c.reg,
               c.refill, ms);

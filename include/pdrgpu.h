@@ -197,8 +197,9 @@ int pdr_chem_solve_batched_noalloc(const pdr_net *net, int ncell, double *d_abun
 
 /* Autotuner: times launch shapes (warps per block, register variant, refill
  * policy) on copies of the first ncell_sample cells of the given inputs (the
- * inputs are not modified) and writes the fastest into opts, keeping its other
- * fields.  Allocates temporary device buffers; call it before stream capture. */
+ * inputs are not modified; the best of two runs per shape) and writes the
+ * fastest into opts, keeping its other fields.  Allocates temporary device
+ * buffers; call it before stream capture. */
 int pdr_chem_autotune(const pdr_net *net, int ncell_sample, const double *d_abundance,
                       const double *d_rate, const double *d_density, pdr_chem_opts *opts,
                       void *stream);
