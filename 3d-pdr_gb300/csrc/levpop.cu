@@ -12,11 +12,12 @@
 //   the solvlevpop matrix (transposed rates, diagonal = -row sum, last row
 //   1e-8, rhs = density*1e-8, solvlevpop.F90:18-35) held in shared memory and
 //   solved either in FP64 by the reference's Gauss-Jordan elimination with full
-//   pivoting (same pivot order, unfused products as in the reference), or by
-//   a row-equilibrated FP32 Gauss-Jordan inverse plus one FP64
-//   iterative-refinement step, verified by the size of the next correction
-//   (cells that fail the check are re-solved in FP64, status 2); negative
-//   populations are set to zero.
+//   pivoting (same pivot order, unfused products as in the reference), or
+//   (mixed) by an FP32 Gauss-Jordan inverse of the row-equilibrated matrix
+//   with partial pivoting and up to two refinement steps, the residual in FP64
+//   and the correction in FP32, each accepted by the size of the next
+//   correction (cells that fail the check are re-solved in FP64, status 2);
+//   negative populations are set to zero.
 #include <algorithm>
 #include <mutex>
 #include <vector>

@@ -257,9 +257,10 @@ int pdr_net_special_reactions(const pdr_net *net, int nr[6]);
  * d_cooling[ncell] (the coolant's cooling_rate), d_line[ncell*nlev*nlev] or
  * NULL, d_status[ncell] (0 ok, 1 singular matrix, 2 mixed solve re-done in
  * FP64) or NULL.  precision PDR_FP64 solves with the reference's full-pivot
- * Gauss-Jordan; PDR_MIXED uses, for coolants of more than 8 levels, a
- * row-equilibrated FP32 Gauss-Jordan inverse plus up to two FP64
- * iterative-refinement steps, accepted when the next correction is below 1e-7
+ * Gauss-Jordan; PDR_MIXED uses, for coolants of more than 8 levels, an FP32
+ * Gauss-Jordan inverse (partial pivoting) of the row-equilibrated matrix plus
+ * up to two refinement steps (FP64 residual, FP32 correction), accepted when
+ * the next correction is below 1e-7
  * of every population above 1e-6 of the coolant density and below 1e-4 of
  * those above 1e-12, and shrinking; other cells are re-solved in FP64 (status
  * 2).  Coolants of up to 8 levels take the FP64 solve in both forms. */
