@@ -25,9 +25,10 @@
 //   PDR_FP64  : M = I - gamma J in FP64, partial-pivot LU (CVDense semantics).
 //   PDR_MIXED : M is formed and factorised in FP32 after the similarity
 //               scaling W M W^-1 with W = diag(1/(rtol|y|+atol)) taken at
-//               setup; the state, RHS, Newton residual and error test stay
-//               FP64.  A cell whose Newton iteration fails with a fresh FP32
-//               matrix is queued and re-solved from its inputs in FP64.
+//               setup, and the Nordsieck columns z2..z5 are FP32; the state,
+//               z1, RHS, Newton residual and error test stay FP64.  A cell
+//               whose Newton iteration keeps failing with a fresh FP32 matrix
+//               is queued and re-solved from its inputs in FP64.
 #include <cstdint>
 #include <mutex>
 #include <type_traits>
