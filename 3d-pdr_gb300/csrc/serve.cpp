@@ -28,6 +28,7 @@
 // Each cell is integrated independently, so a request's results do not depend
 // on what it was batched or overlapped with.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -64,7 +65,9 @@ struct Slot {
   int *d_status = nullptr, *d_rstatus = nullptr;
   std::thread thread;
   bool running = false;
-  int share = 0;   // SMs this slot's launch may keep
+  // SMs this slot's launch may keep: written under the server lock, read by
+  // the slot's own thread between chunks without it
+  std::atomic<int> share{0};
 };
 
 struct Lane {
@@ -178,7 +181,8 @@ int run_batch(pdr_server *s, Lane &L, Slot &S, const std::vector<Req *> &batch) 
     }
     // (a slot outside slot_loop -- the warm-up at creation -- has no share yet:
     // it counts as the whole device; every chunk holds at least one cell)
-    if (s->opts.partition_sms) m = std::min(m, std::max(1, 16 * (S.share > 0 ? S.share : s->sms) * L.cells_per_sm));
+    const int sh = S.share.load(std::memory_order_relaxed);
+    if (s->opts.partition_sms) m = std::min(m, std::max(1, 16 * (sh > 0 ? sh : s->sms) * L.cells_per_sm));
     rc = pdr_solver_run(S.solver, m, S.d_ab + (size_t)c0 * L.nspec, S.d_rate + (size_t)c0 * L.nreac, S.d_nH + c0,
                         S.d_tend + c0, S.d_status + c0, nullptr, st);
     c0 += m;
@@ -212,11 +216,11 @@ int claim_sms(pdr_server *s, Slot &me, bool counted) {
   for (Lane &L : s->lanes)
     for (auto &sp : L.slots) {
       Slot &o = *sp;
-      if (&o == &me || !o.running || o.share <= share) continue;
-      o.share = share;
+      if (&o == &me || !o.running || o.share.load(std::memory_order_relaxed) <= share) continue;
+      o.share.store(share, std::memory_order_relaxed);
       pdr_solver_limit_sms(o.solver, share, s->control);
     }
-  me.share = share;
+  me.share.store(share, std::memory_order_relaxed);
   return share;
 }
 
